@@ -1,0 +1,413 @@
+#!/usr/bin/env python3
+"""Headline benchmark of the lyapunov3d hot path on GB300.
+
+Workload (one "step"): one 1920x1080 frame of the Lyapunov-field raymarch --
+512 steps per ray (step method 1), a seeded 12-symbol sequence over {A,B,C},
+200 settle + 1000 accumulated iterations per sample, parameter cube
+[2, 4]^3, camera uniform on S^3 at distance 5-8 from the cube centre, one
+directional light (scenes.full_render(seed=1)); synthetic inputs, no dataset.
+
+Metric: G logistic-iters/s -- logistic-map iterations the plain method
+performs for the frame (exact per-sample counts from the kernel's statistics)
+divided by the device time of the frame; frames/s beside it.  `value` is
+the chosen form (the renormalised-product lambda); `plain` is the plain
+FP32 drop-in on the same GPU, same frame.  `e2e` is the same metric through
+the host-buffer C-ABI call (lyap_render_host: upload, render, download of
+the RGBA image and the LyapPoint buffer, synchronise), timed on the host.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With --gpus N > 1 (under torchrun) every rank renders the same frame as an
+independent replica (the path does not shard); value = total iterations of
+all ranks / max rank time.  --impl reference times the reference algorithm
+on the host cores instead (the oracle's restatement of the reference's
+arithmetic, all host threads, a bounded band of rows per step).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_FLUSH_BYTES = 512 << 20   # > 129 MB of L2
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--volume", type=int, default=512, help="edge of the secondary volume sweep (0 = skip)")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu), "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            with open(self.path) as f:
+                for line in f:
+                    p = [x.strip() for x in line.split(",")]
+                    if len(p) >= 9:
+                        rows.append(p)
+            os.unlink(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        pw = [num(r[3]) for r in rows if num(r[3])]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(pw) if pw else None}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# --------------------------------------------------------------- CPU arms
+def cpu_render_rate(wl, seconds, threads=0):
+    """The reference algorithm (oracle restatement of the reference's own
+    arithmetic, ORC_REF) on the host cores over seeded rows of the frame
+    until `seconds` of wall time; returns (G iters/s, description, threads)."""
+    from lyapunov3d_gb300 import capi
+    from oracle import ORC_REF, Oracle
+    orc = Oracle()
+    if threads:
+        orc.set_threads(threads)
+    cam = capi.cam_recalculate(wl.cam, wl.width, wl.height, 1)
+    lights = capi.lights_recalculate(wl.lights)
+    seq = capi.seq_parse(wl.seq)
+    rows = np.random.default_rng(12345).permutation(wl.height)
+    iters, t, done = 0, 0.0, 0
+    per = wl.params.settle + wl.params.accum
+    while done < len(rows) and t < seconds:
+        y = int(rows[done])
+        t0 = time.perf_counter()
+        _, _, cnt = orc.render(ORC_REF, wl.width, wl.height, cam, wl.params, seq, lights, y0=y, y1=y + 1)
+        t += time.perf_counter() - t0
+        iters += int(cnt.sum()) * per
+        done += 1
+    desc = (f"{done} of {wl.height} rows (seeded permutation) x {wl.width} px of the frame, reference arithmetic "
+            f"(double-promoted orbit, logf per step), {orc.threads()} OpenMP threads")
+    return iters / t / 1e9, desc, orc.threads(), t
+
+
+def run_reference_arm(args):
+    """--impl reference: the reference algorithm on the host cores, same metric."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from lyapunov3d_gb300 import scenes
+    wl = scenes.full_render(args.seed, args.width, args.height)
+    per_step = max(2.0, min(20.0, 60.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_render_rate(wl, per_step / 4)
+    rates, secs = [], 0.0
+    desc, threads = "", 0
+    for _ in range(args.steps):
+        r, desc, threads, t = cpu_render_rate(wl, per_step)
+        rates.append(r)
+        secs += t
+    value = float(np.mean(rates))
+    frame_iters_est = None
+    line = {
+        "impl": "reference", "metric": "G logistic-iters/s (1080p Lyapunov raymarch frame)", "value": value,
+        "unit": "G iters/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
+        "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "steps_per_ray": 512,
+                   "settle": wl.params.settle, "accum": wl.params.accum, "sequence": wl.seq, "box": [2.0, 4.0]},
+        "cpu_baseline": {"value": value, "unit": "G iters/s", "cores": threads, "kind": "port",
+                         "sample": f"per step: {desc}"},
+        "e2e": {"value": value, "unit": "G iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "host cores only; the reference's GPU path needs its GL front-end and its sources are not on "
+                "this host, so its algorithm runs through the oracle's bit-exact restatement",
+        "frame_iters_est": frame_iters_est,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- GPU arm
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    if not torch.cuda.is_available():
+        print(json.dumps({"error": "no CUDA device"}))
+        sys.exit(1)
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    from lyapunov3d_gb300 import capi, scenes
+    from lyapunov3d_gb300.device import DeviceFrame, DeviceVolume
+
+    wl = scenes.full_render(args.seed, args.width, args.height)
+    frame = DeviceFrame(wl, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed_frames(variant, k, w):
+        """w untimed + k timed frames; each frame timed with its own events, L2 flushed between."""
+        for _ in range(w):
+            frame.run(variant, stream=stream)
+        torch.cuda.synchronize()
+        frame.reset_stats()
+        total_ms = 0.0
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for i in range(k):
+            flush.fill_(float(i))
+            evs[i][0].record(stream)
+            frame.run(variant, stream=stream)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        times = [a.elapsed_time(b) for a, b in evs]
+        total_ms = sum(times)
+        st = frame.stats()
+        return total_ms, times, st
+
+    # pipe-rate probes (the FP32 / MUFU roofline denominators), timed alone
+    sink = torch.zeros(4, dtype=torch.float32, device=dev)
+    probe = {}
+    for kind, name in [(0, "ffma"), (1, "lg2")]:
+        capi.pipe_probe(kind, 64, sink, stream=stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ops = capi.pipe_probe(kind, 512, sink, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        probe[name] = ops / (e0.elapsed_time(e1) * 1e-3)   # lane-ops per second
+
+    S, A = wl.params.settle, wl.params.accum
+    # plain FP32 drop-in, same frame, same GPU
+    barrier()
+    plain_ms, plain_times, plain_st = timed_frames(capi.VARIANT_PLAIN, args.steps, args.warmup)
+    plain_rgba = frame.d_rgba.clone()
+    plain_pts = frame.d_points.clone()
+    # chosen form, with clocks sampled during the timed region
+    barrier()
+    sampler = ClockSampler(local)
+    with sampler:
+        time.sleep(0.3)
+        chosen_ms, chosen_times, chosen_st = timed_frames(capi.VARIANT_PRODUCT, args.steps, args.warmup)
+    clocks = sampler.summary()
+    barrier()
+
+    iters_frame = frame.iterations(chosen_st) // args.steps
+    plain_iters_frame = frame.iterations(plain_st) // args.steps
+
+    # surface agreement and lambda difference between the chosen and the plain frame
+    pts_c = frame.d_points.view(-1, 9).cpu().numpy()
+    pts_p = plain_pts.view(-1, 9).cpu().numpy()
+    hit_c, hit_p = ~np.isnan(pts_c[:, 6]), ~np.isnan(pts_p[:, 6])
+    surf_px = int((hit_c | hit_p).sum())
+    agree = float(((hit_c == hit_p) | ~(hit_c | hit_p)).mean())
+    surf_agree = float((hit_c & hit_p).sum() / max(1, surf_px))
+    both = hit_c & hit_p
+    dl = np.abs(pts_c[both, 8].astype(np.float64) - pts_p[both, 8])
+    lam_diff = {"max_abs": float(dl.max()) if dl.size else 0.0, "mean_abs": float(dl.mean()) if dl.size else 0.0}
+
+    # max over ranks
+    t_chosen = chosen_ms
+    t_plain = plain_ms
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_chosen, t_plain], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_chosen, t_plain = float(tt[0]), float(tt[1])
+
+    value = world * iters_frame * args.steps / (t_chosen * 1e-3) / 1e9
+    plain_value = world * plain_iters_frame * args.steps / (t_plain * 1e-3) / 1e9
+    kernel_ms = statistics.mean(chosen_times)
+    achieved = iters_frame / (kernel_ms * 1e-3) / 1e9
+    # FP32-pipe bound of the chosen (product) form: 2 FP32 ops per settle step,
+    # 4 per accumulated step; the plain form is MUFU-bound at one lg2 per accumulated step
+    peak_fp32 = probe["ffma"] * (S + A) / (2 * S + 4 * A) / 1e9
+    peak_plain = min(probe["lg2"] * (S + A) / A, probe["ffma"] * (S + A) / (2 * S + 4 * A)) / 1e9
+    plain_achieved = plain_iters_frame / (statistics.mean(plain_times) * 1e-3) / 1e9
+
+    # end to end through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        npix = wl.width * wl.height
+        rgba_h = torch.empty(npix * 4, dtype=torch.uint8, pin_memory=True).numpy().reshape(wl.height, wl.width, 4)
+        pts_h = torch.empty(npix * 9, dtype=torch.float32, pin_memory=True).numpy()
+        from lyapunov3d_gb300.types import POINT_DTYPE
+        pts_h = pts_h.view(POINT_DTYPE).reshape(wl.height, wl.width)
+        ext = capi.LyapRenderExt(variant=capi.VARIANT_PRODUCT, light_model=frame.light_model)
+        for _ in range(max(1, args.warmup)):
+            capi.render_host(frame.cam, frame.prm, frame.seq, frame.lights, wl.width, wl.height, ext=ext,
+                             stream=stream, rgba=rgba_h, points=pts_h)
+        e2e_s = 0.0
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            torch.cuda.synchronize()
+            barrier()
+            t0 = time.perf_counter()
+            capi.render_host(frame.cam, frame.prm, frame.seq, frame.lights, wl.width, wl.height, ext=ext,
+                             stream=stream, rgba=rgba_h, points=pts_h)
+            e2e_s += time.perf_counter() - t0
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_s = float(tt[0])
+        e2e = {"value": world * iters_frame * args.steps / e2e_s / 1e9, "unit": "G iters/s",
+               "h2d_bytes_per_step": int(frame.seq.nbytes + 224 * len(frame.lights)),
+               "d2h_bytes_per_step": int(npix * 4 + npix * 36),
+               "frames_per_s": world * args.steps / e2e_s,
+               "call": "lyap_render_host (pinned host buffers; upload, render, download RGBA + LyapPoint, sync)"}
+
+    # secondary: the dense volume sweep (HBM write-out roofline)
+    volume = None
+    if args.volume > 0:
+        vw = scenes.full_volume(args.volume, args.seed)
+        vol = DeviceVolume(vw, device=dev)
+        vol.run(capi.VARIANT_PRODUCT, stream=stream)
+        torch.cuda.synchronize()
+        vol.reset_stats()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(2)]
+        for variant, (e0, e1) in zip([capi.VARIANT_PRODUCT, capi.VARIANT_PLAIN], evs):
+            flush.fill_(0.0)
+            e0.record(stream)
+            vol.run(variant, stream=stream)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        tp, tq = evs[0][0].elapsed_time(evs[0][1]), evs[1][0].elapsed_time(evs[1][1])
+        n = args.volume ** 3
+        vit = n * (S + A)
+        peaks, src = measured_peaks()
+        volume = {"workload": vw.name, "voxels": n, "product_ms": tp, "plain_ms": tq,
+                  "product_g_iters_s": vit / (tp * 1e-3) / 1e9, "plain_g_iters_s": vit / (tq * 1e-3) / 1e9,
+                  "write_gbs": n * 4 / (tp * 1e-3) / 1e9,
+                  "write_frac_of_hbm": n * 4 / (tp * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+        del vol
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        r, desc, threads, t = cpu_render_rate(wl, args.cpu_seconds)
+        cpu = {"value": r, "unit": "G iters/s", "cores": threads, "kind": "port",
+               "sample": desc + f" ({t:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": "G logistic-iters/s (1080p Lyapunov raymarch frame)",
+            "value": value, "unit": "G iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_chosen / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
+            "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "steps_per_ray": 512,
+                       "step_method": 1, "settle": S, "accum": A, "sequence": wl.seq, "box": [2.0, 4.0],
+                       "variant": "product (renormalised FP32 product, one log2 per sample)",
+                       "l2": f"flushed between timed frames ({L2_FLUSH_BYTES >> 20} MiB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "frames_per_s": world * args.steps / (t_chosen * 1e-3),
+            "iters_per_frame": iters_frame,
+            "samples_per_frame": int(chosen_st[capi.STAT_SAMPLES]) // args.steps,
+            "hits_per_frame": int(chosen_st[capi.STAT_HITS]) // args.steps,
+            "plain": {"value": plain_value, "unit": "G iters/s", "ms_per_step": t_plain / args.steps,
+                      "frames_per_s": world * args.steps / (t_plain * 1e-3),
+                      "roofline_frac": plain_achieved / peak_plain},
+            "speedup_vs_plain": value / plain_value,
+            "surface": {"pixel_agreement": agree, "surface_pixel_agreement": surf_agree,
+                        "lambda_at_hits_vs_plain": lam_diff},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "G iters/s",
+                         "frac": achieved / peak_fp32, "traffic": None,
+                         "peak_source": "measured live: FFMA pipe-rate probe (lyap_pipe_probe) x (S+A)/(2S+4A) "
+                                        "FP32 ops per iteration",
+                         "probe_ffma_tops": probe["ffma"] / 1e12, "probe_lg2_tops": probe["lg2"] / 1e12,
+                         "kernel": "render_persistent<MODE_PRODUCT>"},
+            "e2e": e2e,
+            "volume": volume,
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -177,6 +177,123 @@ LYAP_STATIC_ASSERT(sizeof(LyapParamsD) == 104, "LyapParamsD size");
 LYAP_STATIC_ASSERT(offsetof(LyapParamsD, nearThreshold) == 24, "LyapParamsD.nearThreshold");
 LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 
+/* ---- extensions (kept out of the reference structs) -------------------- */
+#define LYAP_VERSION_STRING "0.1.0"
+#define LYAP_MAX_PIXELS  (1ull << 31)    /* per frame */
+#define LYAP_MAX_VOXELS  (1ull << 36)    /* per volume (256 GiB of float) */
+
+/* How lambda is accumulated.  Both iterate the orbit identically
+ * (t = r*x; x = fma(-t, x, t); d = fma(-2r, x, r)). */
+#define LYAP_VARIANT_PLAIN   0u  /* sum of log2|d| per step (the drop-in)    */
+#define LYAP_VARIANT_PRODUCT 1u  /* running product of |d|, renormalised by
+                                    exponent extraction every 8 steps, one
+                                    log2 at the end                          */
+
+#define LYAP_LIGHT_SPOT        0u /* the reference's shade() (kernel.cu:25)  */
+#define LYAP_LIGHT_DIRECTIONAL 1u /* Lambert: ambient + diffuse*clamp(N.-V)  */
+
+/* Slots of the optional statistics array (LyapRenderExt / LyapVolumeExt
+ * d_stats, 8 x uint64, accumulated with atomics; the caller zeroes it).
+ * Logistic-map iterations performed = SAMPLES*(settle+accum) - SKIPPED*accum. */
+#define LYAP_STAT_SAMPLES  0  /* lambda evaluations                          */
+#define LYAP_STAT_SKIPPED  1  /* evaluations whose settle landed on x = 0.5  */
+#define LYAP_STAT_MARCH    2  /* render: march samples                       */
+#define LYAP_STAT_HONE     3  /* render: honing samples                      */
+#define LYAP_STAT_NORMAL   4  /* render: normal samples                      */
+#define LYAP_STAT_HITS     5  /* render: rays that hit                       */
+#define LYAP_STAT_RAYS     6  /* render: rays finished                       */
+#define LYAP_STAT_FALLBACK 7  /* product evaluations redone in plain form    */
+#define LYAP_STAT_COUNT    8
+
+typedef struct {
+    uint32_t size;               /* = sizeof(LyapRenderExt) */
+    uint32_t variant;            /* LYAP_VARIANT_* (default PLAIN) */
+    uint32_t light_model;        /* LYAP_LIGHT_* (default SPOT) */
+    uint32_t flags;              /* reserved, 0 */
+    uint32_t *d_counts;          /* optional device array, 3 per pixel:
+                                    march, honing, normal samples */
+    unsigned long long *d_stats; /* optional device array, LYAP_STAT_COUNT */
+    uint32_t blocks_per_sm;      /* launch shape, 0 = automatic */
+    uint32_t threads_per_block;  /* multiple of 32, <= 128; 0 = automatic */
+} LyapRenderExt;
+
+typedef struct {
+    uint32_t size;               /* = sizeof(LyapVolumeExt) */
+    uint32_t variant;            /* LYAP_VARIANT_* */
+    unsigned long long *d_stats; /* optional, LYAP_STAT_COUNT */
+    uint32_t blocks_per_sm;      /* 0 = automatic */
+    uint32_t threads_per_block;  /* multiple of 32, <= 256; 0 = automatic */
+} LyapVolumeExt;
+
+/* ---- entry points ------------------------------------------------------ */
+
+int lyap_abi_version(void);
+const char *lyap_version(void);
+/* Message of the calling thread's last failure ("" if none). */
+const char *lyap_last_error_string(void);
+const char *lyap_status_string(int code);
+
+/* scene_convert_sequence (scene.cu:69; declared scene.hpp:11).  Letters A-D
+ * (any case) give symbols 0-3, a digit k repeats the previous letter k more
+ * times (B before any letter), a -1 terminator is appended.  *len receives
+ * the entry count including the -1.  A bad character gives
+ * LYAP_ERR_SEQUENCE (the reference exits); a short buffer LYAP_ERR_CAPACITY. */
+int lyap_seq_parse(const char *str, int32_t *out, size_t cap, size_t *len);
+
+/* scene_cam_recalculate (scene.cu:31; scene.hpp:13): fills V, S0, SDX, SDY,
+ * the render size (texture size / denominator) and the cones of `cam`;
+ * tw/th/td of 0 keep the current values. */
+int lyap_cam_recalculate(LyapCam *cam, uint32_t tw, uint32_t th, uint32_t td);
+
+/* scene_lights_recalculate (scene.cu:20; scene.hpp:15): axis V and cones. */
+int lyap_lights_recalculate(LyapLight *lights, size_t n);
+
+/* kernel_calc_render (kernel.cu:500; launched at lyap_interactive.cu:711)
+ * over a width x height image, pixel (x, y) at index x + y*width.  `cam`
+ * and `prm` are host structs (by value in the reference); d_seq (seq_len
+ * entries incl. the -1), d_lights, d_rgba and d_points are device memory.
+ * A hit writes its LyapPoint; a miss writes an all-NaN point and RGBA 0.
+ * Colour bytes saturate.  Every row is rendered.  Asynchronous on stream. */
+int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
+                const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
+                uint32_t width, uint32_t height, const LyapRenderExt *ext, void *stream);
+
+/* kernel_calc_volume (kernel.cu:518; launched at lyap_calculate.cu:72):
+ * lambda at (lo + (hi-lo)*i/n) per axis, x fastest, into d_out[nx*ny*nz].
+ * lo/hi (3 floats each) may be NULL for the reference's [0, 4).  */
+int lyap_volume(float *d_out, uint32_t nx, uint32_t ny, uint32_t nz, const float *lo, const float *hi,
+                const LyapParams *prm, const int32_t *d_seq, size_t seq_len, const LyapVolumeExt *ext,
+                void *stream);
+
+/* Host-buffer forms of the two above (the reference front-ends' whole
+ * round trip: upload, launch, download; lyap_interactive.cu:696-741,
+ * lyap_calculate.cu:58-91).  seq / lights are host arrays, outputs are host
+ * memory (points may be NULL); returns after the stream is synchronised. */
+int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *seq, size_t seq_len,
+                     const LyapLight *lights, uint32_t n_lights, RGBA *rgba, LyapPoint *points,
+                     uint32_t width, uint32_t height, const LyapRenderExt *ext, void *stream);
+int lyap_volume_host(float *out, uint32_t nx, uint32_t ny, uint32_t nz, const float *lo, const float *hi,
+                     const LyapParams *prm, const int32_t *seq, size_t seq_len, const LyapVolumeExt *ext,
+                     void *stream);
+
+/* The reference's own __global__ entry points (lyap_kernel.hpp) launched
+ * with an explicit launch shape, for callers without <<<>>>: exactly
+ * kernel_calc_render<<<(grid_x, grid_y), (block_x, block_y)>>>
+ * (lyap_interactive.cu:711) and kernel_calc_volume<<<grid, block>>>
+ * (lyap_calculate.cu:72), with their index and coordinate conventions
+ * (image width / volume extents = grid * block).  Plain FP32. */
+int lyap_kernel_calc_render(uint32_t grid_x, uint32_t grid_y, uint32_t block_x, uint32_t block_y,
+                            RGBA *d_rgba, LyapPoint *d_points, const LyapCam *cam, const LyapParams *prm,
+                            int32_t *d_seq, LyapLight *d_lights, uint32_t n_lights, void *stream);
+int lyap_kernel_calc_volume(const uint32_t grid[3], const uint32_t block[3], float *d_exps,
+                            const LyapParams *prm, int32_t *d_seq, void *stream);
+
+/* Measurement support (no reference counterpart): a pipe-rate probe whose
+ * launch the caller times.  kind 0 = dependent-chain-free FFMA, kind 1 =
+ * lg2.approx; *ops receives the operations performed.  The rate is the
+ * denominator of the lambda kernels' FP32 / MUFU roofline. */
+int lyap_pipe_probe(uint32_t kind, uint32_t iters, float *d_sink, double *ops, void *stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

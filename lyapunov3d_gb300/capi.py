@@ -1,0 +1,229 @@
+"""ctypes binding of the C ABI (include/lyap_gb300.h).
+
+Every call goes to the in-tree library lyapunov3d_gb300/_lib/liblyap_gb300.so;
+if it is missing the import of this module fails loudly (there is no CPU
+fallback).  A non-zero status from the library raises LyapError carrying the
+library's own message.  Device pointers are plain integers (e.g. a torch
+tensor's data_ptr()); streams are cudaStream_t handles as integers (0 = the
+legacy default stream).
+"""
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_float, c_int, c_int32, c_size_t, c_uint32, c_void_p
+
+import numpy as np
+
+from .types import LyapCam, LyapLight, LyapParams, POINT_DTYPE, RGBA_DTYPE
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", "liblyap_gb300.so")
+
+LYAP_OK = 0
+LYAP_ERR_INVALID_ARG = -1
+LYAP_ERR_SEQUENCE = -2
+LYAP_ERR_CUDA = -3
+LYAP_ERR_NO_DEVICE = -4
+LYAP_ERR_OUT_OF_MEMORY = -5
+LYAP_ERR_CAPACITY = -6
+
+VARIANT_PLAIN = 0
+VARIANT_PRODUCT = 1
+LIGHT_SPOT = 0
+LIGHT_DIRECTIONAL = 1
+MAX_SEQ_LEN = 4096
+MAX_LIGHTS = 16
+
+STAT_SAMPLES, STAT_SKIPPED, STAT_MARCH, STAT_HONE, STAT_NORMAL, STAT_HITS, STAT_RAYS, STAT_FALLBACK = range(8)
+STAT_COUNT = 8
+
+
+class LyapError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+        self.message = message
+
+
+class LyapRenderExt(ctypes.Structure):
+    _fields_ = [("size", c_uint32), ("variant", c_uint32), ("light_model", c_uint32), ("flags", c_uint32),
+                ("d_counts", c_void_p), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
+                ("threads_per_block", c_uint32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.size = ctypes.sizeof(LyapRenderExt)
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+class LyapVolumeExt(ctypes.Structure):
+    _fields_ = [("size", c_uint32), ("variant", c_uint32), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
+                ("threads_per_block", c_uint32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.size = ctypes.sizeof(LyapVolumeExt)
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+# every extern "C" symbol include/lyap_gb300.h declares (checked by tests)
+EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string",
+            "lyap_seq_parse", "lyap_cam_recalculate", "lyap_lights_recalculate", "lyap_render",
+            "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
+            "lyap_kernel_calc_volume", "lyap_pipe_probe"]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m lyapunov3d_gb300.build` "
+                          "(or __graft_entry__.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    L.lyap_abi_version.restype = c_int
+    L.lyap_version.restype = c_char_p
+    L.lyap_last_error_string.restype = c_char_p
+    L.lyap_status_string.restype = c_char_p
+    L.lyap_status_string.argtypes = [c_int]
+    L.lyap_seq_parse.argtypes = [c_char_p, POINTER(c_int32), c_size_t, POINTER(c_size_t)]
+    L.lyap_cam_recalculate.argtypes = [c_void_p, c_uint32, c_uint32, c_uint32]
+    L.lyap_lights_recalculate.argtypes = [c_void_p, c_size_t]
+    L.lyap_render.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_uint32, c_void_p, c_void_p,
+                              c_uint32, c_uint32, c_void_p, c_void_p]
+    L.lyap_volume.argtypes = [c_void_p, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p,
+                              c_size_t, c_void_p, c_void_p]
+    L.lyap_render_host.argtypes = L.lyap_render.argtypes
+    L.lyap_volume_host.argtypes = L.lyap_volume.argtypes
+    L.lyap_kernel_calc_render.argtypes = [c_uint32] * 4 + [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                                           c_void_p, c_uint32, c_void_p]
+    L.lyap_kernel_calc_volume.argtypes = [POINTER(c_uint32), POINTER(c_uint32), c_void_p, c_void_p, c_void_p,
+                                          c_void_p]
+    L.lyap_pipe_probe.argtypes = [c_uint32, c_uint32, c_void_p, POINTER(ctypes.c_double), c_void_p]
+    for name in EXPORTED:
+        if name not in ("lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string"):
+            getattr(L, name).restype = c_int
+    return L
+
+
+lib = _load()
+
+
+def _check(rc):
+    if rc != LYAP_OK:
+        raise LyapError(rc, lib.lyap_last_error_string().decode(errors="replace"))
+    return rc
+
+
+def version():
+    return lib.lyap_version().decode()
+
+
+def last_error():
+    return lib.lyap_last_error_string().decode(errors="replace")
+
+
+def _vp(p):
+    if p is None:
+        return None
+    if hasattr(p, "data_ptr"):
+        return c_void_p(p.data_ptr())
+    if isinstance(p, np.ndarray):
+        return c_void_p(p.ctypes.data)
+    return c_void_p(int(p))
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if hasattr(s, "cuda_stream"):
+        return c_void_p(s.cuda_stream)
+    return c_void_p(int(s))
+
+
+# ---- host scene helpers (scene.hpp:11-15) -------------------------------
+def seq_parse(s, cap=MAX_SEQ_LEN):
+    """scene_convert_sequence: the -1 terminated symbol array (np.int32)."""
+    out = (c_int32 * cap)()
+    n = c_size_t(0)
+    _check(lib.lyap_seq_parse(s.encode() if isinstance(s, str) else s, out, cap, ctypes.byref(n)))
+    return np.array(out[:n.value], dtype=np.int32)
+
+
+def cam_recalculate(cam, tw, th, td=1):
+    """scene_cam_recalculate on a copy of cam; returns the copy."""
+    c = LyapCam.from_buffer_copy(cam)
+    _check(lib.lyap_cam_recalculate(ctypes.byref(c), tw, th, td))
+    return c
+
+
+def lights_recalculate(lights):
+    arr = (LyapLight * max(1, len(lights)))(*[LyapLight.from_buffer_copy(l) for l in lights])
+    _check(lib.lyap_lights_recalculate(arr, len(lights)))
+    return list(arr)[:len(lights)]
+
+
+def lights_array(lights):
+    """LyapLight[] as a numpy byte array (for upload)."""
+    arr = (LyapLight * max(1, len(lights)))(*[LyapLight.from_buffer_copy(l) for l in lights])
+    return np.frombuffer(bytes(arr), dtype=np.uint8)[:ctypes.sizeof(LyapLight) * len(lights)].copy()
+
+
+# ---- device entry points --------------------------------------------------
+def render(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext=None, stream=None):
+    """lyap_render: asynchronous on `stream`; pointers are device addresses."""
+    _check(lib.lyap_render(ctypes.byref(cam), ctypes.byref(prm), _vp(d_seq), seq_len, _vp(d_lights), n_lights,
+                           _vp(d_rgba), _vp(d_points), width, height,
+                           ctypes.byref(ext) if ext is not None else None, _stream(stream)))
+
+
+def volume(d_out, nx, ny, nz, lo, hi, prm, d_seq, seq_len, ext=None, stream=None):
+    lo_a = (c_float * 3)(*lo) if lo is not None else None
+    hi_a = (c_float * 3)(*hi) if hi is not None else None
+    _check(lib.lyap_volume(_vp(d_out), nx, ny, nz, lo_a, hi_a, ctypes.byref(prm), _vp(d_seq), seq_len,
+                           ctypes.byref(ext) if ext is not None else None, _stream(stream)))
+
+
+def kernel_calc_render(grid, block, d_rgba, d_points, cam, prm, d_seq, d_lights, n_lights, stream=None):
+    """kernel_calc_render<<<grid, block>>> (the reference's entry point and launch shape)."""
+    _check(lib.lyap_kernel_calc_render(grid[0], grid[1], block[0], block[1], _vp(d_rgba), _vp(d_points),
+                                       ctypes.byref(cam), ctypes.byref(prm), _vp(d_seq), _vp(d_lights), n_lights,
+                                       _stream(stream)))
+
+
+def kernel_calc_volume(grid, block, d_exps, prm, d_seq, stream=None):
+    """kernel_calc_volume<<<grid, block>>> (the reference's entry point and launch shape)."""
+    g = (c_uint32 * 3)(*grid)
+    b = (c_uint32 * 3)(*block)
+    _check(lib.lyap_kernel_calc_volume(g, b, _vp(d_exps), ctypes.byref(prm), _vp(d_seq), _stream(stream)))
+
+
+def pipe_probe(kind, iters, d_sink, stream=None):
+    """Launch the FFMA (kind 0) or lg2 (kind 1) rate probe; returns the op count."""
+    ops = ctypes.c_double(0)
+    _check(lib.lyap_pipe_probe(kind, iters, _vp(d_sink), ctypes.byref(ops), _stream(stream)))
+    return ops.value
+
+
+def render_host(cam, prm, seq, lights, width, height, ext=None, stream=None, rgba=None, points=None,
+                want_points=True):
+    """lyap_render_host with numpy buffers; returns (rgba[h, w, 4] u8, points[h, w] or None)."""
+    seq = np.ascontiguousarray(seq, dtype=np.int32)
+    la = lights_array(lights)
+    if rgba is None:
+        rgba = np.empty((height, width, 4), dtype=np.uint8)
+    if want_points and points is None:
+        points = np.empty((height, width), dtype=POINT_DTYPE)
+    _check(lib.lyap_render_host(ctypes.byref(cam), ctypes.byref(prm), _vp(seq), seq.size, _vp(la), len(lights),
+                                _vp(rgba), _vp(points) if want_points else None, width, height,
+                                ctypes.byref(ext) if ext is not None else None, _stream(stream)))
+    return rgba, points
+
+
+def volume_host(nx, ny, nz, prm, seq, lo=None, hi=None, ext=None, stream=None, out=None):
+    seq = np.ascontiguousarray(seq, dtype=np.int32)
+    if out is None:
+        out = np.empty((nz, ny, nx), dtype=np.float32)
+    lo_a = (c_float * 3)(*lo) if lo is not None else None
+    hi_a = (c_float * 3)(*hi) if hi is not None else None
+    _check(lib.lyap_volume_host(_vp(out), nx, ny, nz, lo_a, hi_a, ctypes.byref(prm), _vp(seq), seq.size,
+                                ctypes.byref(ext) if ext is not None else None, _stream(stream)))
+    return out

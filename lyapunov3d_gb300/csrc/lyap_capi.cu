@@ -1,0 +1,288 @@
+// lyap_capi.cu -- the C ABI (include/lyap_gb300.h): argument checking, error
+// reporting, scratch management and the host-buffer wrappers.  Nothing here
+// exits the process (the reference's helper_cuda checks do); every failure
+// returns a negative LYAP_ERR_* code and leaves a message for
+// lyap_last_error_string().
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+
+#include "lyap_device.cuh"
+#include "lyap_gb300.h"
+#include "lyap_internal.h"
+
+namespace lyapgb {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_error(cudaError_t e, const char *what)
+{
+    int code = LYAP_ERR_CUDA;
+    if (e == cudaErrorMemoryAllocation) code = LYAP_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice ||
+        e == cudaErrorInvalidDevice)
+        code = LYAP_ERR_NO_DEVICE;
+    return set_error(code, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+static int check_params(const LyapParams *prm, const char *fn)
+{
+    if (!prm) return set_error(LYAP_ERR_INVALID_ARG, "%s: null params", fn);
+    return LYAP_OK;
+}
+
+static int check_seq_len(size_t seq_len, const char *fn)
+{
+    if (seq_len < 2 || seq_len > LYAP_MAX_SEQ_LEN)
+        return set_error(LYAP_ERR_SEQUENCE, "%s: seq_len %zu outside [2, %d] (entries incl. the -1)", fn, seq_len,
+                         LYAP_MAX_SEQ_LEN);
+    return LYAP_OK;
+}
+
+static int check_host_seq(const int32_t *seq, size_t seq_len, const char *fn)
+{
+    if (!seq) return set_error(LYAP_ERR_INVALID_ARG, "%s: null sequence", fn);
+    int rc = check_seq_len(seq_len, fn);
+    if (rc) return rc;
+    for (size_t i = 0; i + 1 < seq_len; i++)
+        if (seq[i] < 0 || seq[i] > 3)
+            return set_error(LYAP_ERR_SEQUENCE, "%s: symbol %d at %zu is not 0..3", fn, seq[i], i);
+    if (seq[seq_len - 1] != -1) return set_error(LYAP_ERR_SEQUENCE, "%s: sequence is not -1 terminated", fn);
+    return LYAP_OK;
+}
+
+static int check_ext_render(const LyapRenderExt *ext, const char *fn)
+{
+    if (!ext) return LYAP_OK;
+    if (ext->size != sizeof(LyapRenderExt))
+        return set_error(LYAP_ERR_INVALID_ARG, "%s: LyapRenderExt.size is %u, expected %zu", fn, ext->size,
+                         sizeof(LyapRenderExt));
+    if (ext->variant > LYAP_VARIANT_PRODUCT) return set_error(LYAP_ERR_INVALID_ARG, "%s: unknown variant %u", fn, ext->variant);
+    if (ext->light_model > LYAP_LIGHT_DIRECTIONAL)
+        return set_error(LYAP_ERR_INVALID_ARG, "%s: unknown light model %u", fn, ext->light_model);
+    if (ext->threads_per_block && (ext->threads_per_block % 32 || ext->threads_per_block > 128))
+        return set_error(LYAP_ERR_INVALID_ARG, "%s: threads_per_block must be a multiple of 32, at most 128", fn);
+    return LYAP_OK;
+}
+
+static int check_ext_volume(const LyapVolumeExt *ext, const char *fn)
+{
+    if (!ext) return LYAP_OK;
+    if (ext->size != sizeof(LyapVolumeExt))
+        return set_error(LYAP_ERR_INVALID_ARG, "%s: LyapVolumeExt.size is %u, expected %zu", fn, ext->size,
+                         sizeof(LyapVolumeExt));
+    if (ext->variant > LYAP_VARIANT_PRODUCT) return set_error(LYAP_ERR_INVALID_ARG, "%s: unknown variant %u", fn, ext->variant);
+    if (ext->threads_per_block && (ext->threads_per_block % 32 || ext->threads_per_block > 256))
+        return set_error(LYAP_ERR_INVALID_ARG, "%s: threads_per_block must be a multiple of 32, at most 256", fn);
+    return LYAP_OK;
+}
+
+static int check_render_args(const LyapCam *cam, const LyapParams *prm, const void *seq, size_t seq_len,
+                             const void *lights, uint32_t n_lights, const void *rgba, const void *points,
+                             uint32_t width, uint32_t height, const LyapRenderExt *ext, const char *fn)
+{
+    if (!cam) return set_error(LYAP_ERR_INVALID_ARG, "%s: null camera", fn);
+    int rc = check_params(prm, fn);
+    if (rc) return rc;
+    if (!seq) return set_error(LYAP_ERR_INVALID_ARG, "%s: null sequence", fn);
+    if ((rc = check_seq_len(seq_len, fn))) return rc;
+    if (n_lights > LYAP_MAX_LIGHTS) return set_error(LYAP_ERR_INVALID_ARG, "%s: %u lights > %d", fn, n_lights, LYAP_MAX_LIGHTS);
+    if (n_lights && !lights) return set_error(LYAP_ERR_INVALID_ARG, "%s: null lights", fn);
+    if (!rgba) return set_error(LYAP_ERR_INVALID_ARG, "%s: null rgba output", fn);
+    if (!points) return set_error(LYAP_ERR_INVALID_ARG, "%s: null points output", fn);
+    if (width == 0 || height == 0) return set_error(LYAP_ERR_INVALID_ARG, "%s: zero image size %ux%u", fn, width, height);
+    if ((uint64_t)width * height > LYAP_MAX_PIXELS)
+        return set_error(LYAP_ERR_INVALID_ARG, "%s: %ux%u exceeds %llu pixels", fn, width, height,
+                         (unsigned long long)LYAP_MAX_PIXELS);
+    return check_ext_render(ext, fn);
+}
+
+static RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
+                          const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
+                          uint32_t width, uint32_t height, const LyapRenderExt *ext)
+{
+    RenderJob job;
+    memset(&job, 0, sizeof(job));
+    job.cam = *cam;
+    job.prm = *prm;
+    job.seq = d_seq;
+    job.lights = d_lights;
+    job.rgba = d_rgba;
+    job.points = d_points;
+    job.counts = ext ? ext->d_counts : nullptr;
+    job.seq_period = (uint32_t)(seq_len - 1);
+    job.n_lights = n_lights;
+    job.width = width;
+    job.height = height;
+    job.light_model = ext ? ext->light_model : LYAP_LIGHT_SPOT;
+    return job;
+}
+
+}  // namespace lyapgb
+
+using namespace lyapgb;
+
+extern "C" {
+
+int lyap_abi_version(void) { return LYAP_ABI_VERSION; }
+
+const char *lyap_version(void) { return "lyapunov3d_gb300 " LYAP_VERSION_STRING " (sm_103a)"; }
+
+const char *lyap_last_error_string(void) { return g_err; }
+
+const char *lyap_status_string(int code)
+{
+    switch (code) {
+    case LYAP_OK: return "ok";
+    case LYAP_ERR_INVALID_ARG: return "invalid argument";
+    case LYAP_ERR_SEQUENCE: return "bad sequence";
+    case LYAP_ERR_CUDA: return "CUDA error";
+    case LYAP_ERR_NO_DEVICE: return "no usable sm_103 device";
+    case LYAP_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case LYAP_ERR_CAPACITY: return "output buffer too small";
+    default: return "unknown status";
+    }
+}
+
+int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
+                const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points, uint32_t width,
+                uint32_t height, const LyapRenderExt *ext, void *stream)
+{
+    int rc = check_render_args(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext,
+                               "lyap_render");
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    RenderJob job = make_job(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext);
+    // scratch: the pixel queue's counter, stream-ordered so concurrent calls
+    // on different streams each get their own
+    uint32_t *d_counter = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&d_counter, sizeof(uint32_t), s);
+    if (e != cudaSuccess) return cuda_error(e, "lyap_render: scratch allocation");
+    e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s);
+    if (e == cudaSuccess)
+        e = launch_render(job, ext ? ext->variant : LYAP_VARIANT_PLAIN, d_counter, ext ? ext->d_stats : nullptr,
+                          ext ? ext->blocks_per_sm : 0, ext ? ext->threads_per_block : 0, s);
+    cudaError_t e2 = cudaFreeAsync(d_counter, s);
+    if (e != cudaSuccess) return cuda_error(e, "lyap_render: launch");
+    if (e2 != cudaSuccess) return cuda_error(e2, "lyap_render: scratch release");
+    return LYAP_OK;
+}
+
+int lyap_volume(float *d_out, uint32_t nx, uint32_t ny, uint32_t nz, const float *lo, const float *hi,
+                const LyapParams *prm, const int32_t *d_seq, size_t seq_len, const LyapVolumeExt *ext, void *stream)
+{
+    int rc = check_params(prm, "lyap_volume");
+    if (rc) return rc;
+    if (!d_out) return set_error(LYAP_ERR_INVALID_ARG, "lyap_volume: null output");
+    if (!d_seq) return set_error(LYAP_ERR_INVALID_ARG, "lyap_volume: null sequence");
+    if ((rc = check_seq_len(seq_len, "lyap_volume"))) return rc;
+    if (nx == 0 || ny == 0 || nz == 0) return set_error(LYAP_ERR_INVALID_ARG, "lyap_volume: zero dimension");
+    if ((uint64_t)nx * ny * nz > LYAP_MAX_VOXELS)
+        return set_error(LYAP_ERR_INVALID_ARG, "lyap_volume: %ux%ux%u exceeds %llu voxels", nx, ny, nz,
+                         (unsigned long long)LYAP_MAX_VOXELS);
+    if ((rc = check_ext_volume(ext, "lyap_volume"))) return rc;
+    VolumeJob job;
+    memset(&job, 0, sizeof(job));
+    job.out = d_out;
+    job.seq = d_seq;
+    job.prm = *prm;
+    job.seq_period = (uint32_t)(seq_len - 1);
+    job.nx = nx;
+    job.ny = ny;
+    job.nz = nz;
+    for (int k = 0; k < 3; k++) {
+        job.lo[k] = lo ? lo[k] : 0.0f;   // kernel.cu:527-529: [0, 4) when not given
+        job.hi[k] = hi ? hi[k] : 4.0f;
+    }
+    cudaError_t e = launch_volume(job, ext ? ext->variant : LYAP_VARIANT_PLAIN, ext ? ext->d_stats : nullptr,
+                                  ext ? ext->blocks_per_sm : 0, ext ? ext->threads_per_block : 0,
+                                  (cudaStream_t)stream);
+    if (e != cudaSuccess) return cuda_error(e, "lyap_volume: launch");
+    return LYAP_OK;
+}
+
+int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *seq, size_t seq_len,
+                     const LyapLight *lights, uint32_t n_lights, RGBA *rgba, LyapPoint *points, uint32_t width,
+                     uint32_t height, const LyapRenderExt *ext, void *stream)
+{
+    int rc = check_render_args(cam, prm, seq, seq_len, lights, n_lights, rgba, (void *)1, width, height, ext,
+                               "lyap_render_host");
+    if (rc) return rc;
+    if ((rc = check_host_seq(seq, seq_len, "lyap_render_host"))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t npix = (size_t)width * height;
+    const size_t seq_b = seq_len * sizeof(int32_t), light_b = (size_t)n_lights * sizeof(LyapLight);
+    const size_t rgba_b = npix * sizeof(RGBA), pts_b = npix * sizeof(LyapPoint);
+    // one device block: [seq | lights | rgba | points], 256-byte aligned parts
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t off_l = up(seq_b), off_r = off_l + up(light_b), off_p = off_r + up(rgba_b);
+    const size_t total = off_p + up(pts_b);
+    char *dev = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&dev, total, s);
+    if (e != cudaSuccess) return cuda_error(e, "lyap_render_host: device buffers");
+    e = cudaMemcpyAsync(dev, seq, seq_b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && light_b) e = cudaMemcpyAsync(dev + off_l, lights, light_b, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        rc = lyap_render(cam, prm, (const int32_t *)dev, seq_len, (const LyapLight *)(dev + off_l), n_lights,
+                         (RGBA *)(dev + off_r), (LyapPoint *)(dev + off_p), width, height, ext, stream);
+        if (rc) {
+            cudaFreeAsync(dev, s);
+            return rc;
+        }
+        e = cudaMemcpyAsync(rgba, dev + off_r, rgba_b, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && points) e = cudaMemcpyAsync(points, dev + off_p, pts_b, cudaMemcpyDeviceToHost, s);
+    }
+    cudaError_t e2 = cudaFreeAsync(dev, s);
+    cudaError_t e3 = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_error(e, "lyap_render_host: copies");
+    if (e2 != cudaSuccess) return cuda_error(e2, "lyap_render_host: release");
+    if (e3 != cudaSuccess) return cuda_error(e3, "lyap_render_host: synchronize");
+    return LYAP_OK;
+}
+
+int lyap_volume_host(float *out, uint32_t nx, uint32_t ny, uint32_t nz, const float *lo, const float *hi,
+                     const LyapParams *prm, const int32_t *seq, size_t seq_len, const LyapVolumeExt *ext,
+                     void *stream)
+{
+    int rc = check_host_seq(seq, seq_len, "lyap_volume_host");
+    if (rc) return rc;
+    if (!out) return set_error(LYAP_ERR_INVALID_ARG, "lyap_volume_host: null output");
+    if (nx == 0 || ny == 0 || nz == 0) return set_error(LYAP_ERR_INVALID_ARG, "lyap_volume_host: zero dimension");
+    if ((uint64_t)nx * ny * nz > LYAP_MAX_VOXELS)
+        return set_error(LYAP_ERR_INVALID_ARG, "lyap_volume_host: %ux%ux%u exceeds %llu voxels", nx, ny, nz,
+                         (unsigned long long)LYAP_MAX_VOXELS);
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t out_b = (size_t)nx * ny * nz * sizeof(float);
+    const size_t seq_off = (out_b + 255) & ~(size_t)255;
+    char *dev = nullptr;
+    cudaError_t e = cudaMallocAsync((void **)&dev, seq_off + seq_len * sizeof(int32_t), s);
+    if (e != cudaSuccess) return cuda_error(e, "lyap_volume_host: device buffers");
+    e = cudaMemcpyAsync(dev + seq_off, seq, seq_len * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        rc = lyap_volume((float *)dev, nx, ny, nz, lo, hi, prm, (const int32_t *)(dev + seq_off), seq_len, ext, stream);
+        if (rc) {
+            cudaFreeAsync(dev, s);
+            return rc;
+        }
+        e = cudaMemcpyAsync(out, dev, out_b, cudaMemcpyDeviceToHost, s);
+    }
+    cudaError_t e2 = cudaFreeAsync(dev, s);
+    cudaError_t e3 = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_error(e, "lyap_volume_host: copies");
+    if (e2 != cudaSuccess) return cuda_error(e2, "lyap_volume_host: release");
+    if (e3 != cudaSuccess) return cuda_error(e3, "lyap_volume_host: synchronize");
+    return LYAP_OK;
+}
+
+}  // extern "C"

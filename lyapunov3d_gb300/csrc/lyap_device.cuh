@@ -1,0 +1,573 @@
+// lyap_device.cuh -- device-side building blocks of the hot path (sm_103a).
+//
+//  * per-ray arithmetic (ray setup, box slab test, march / hone / normal
+//    state machine, shading) that rounds every operation exactly as the
+//    reference's host build does (kernel.cu:25-486): this translation unit
+//    is compiled with -fmad=false, IEEE division and square root, and uses
+//    double precision wherever a double literal in the reference promotes
+//    the expression.  Ray positions and step decisions are therefore
+//    bit-identical to the oracle's whenever the lambda values agree;
+//  * the lambda evaluators (kernel.cu:108-154), the only hot loop:
+//      MODE_PLAIN   -- one lg2.approx per accumulated step (the drop-in);
+//      MODE_PRODUCT -- running FP32 product of |r(1-2x)| renormalised by
+//                      exponent extraction every 8 steps, one lg2 at the end.
+//    Both iterate the orbit identically: t = r*x; x = fma(-t, x, t);
+//    d = fma(-2r, x, r).  The sequence symbol at every step is warp-uniform,
+//    so for periods up to 16 the loop is unrolled over whole periods with
+//    the four candidate values of r held in registers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lyap_gb300.h"
+
+namespace lyapgb {
+
+constexpr uint32_t MODE_PLAIN = 0;
+constexpr uint32_t MODE_PRODUCT = 1;
+
+constexpr uint32_t HONE_CAP = 256;          // honing samples per ray
+constexpr uint32_t MARCH_MAX = 4194304u;    // march samples per ray
+constexpr float LN2F = 0.693147180559945309417232121458f;
+
+// statistics slots (LYAP_STAT_* in lyap_gb300.h)
+constexpr int ST_SAMPLES = 0, ST_SKIPPED = 1, ST_MARCH = 2, ST_HONE = 3, ST_NORMAL = 4,
+              ST_HITS = 5, ST_RAYS = 6, ST_FALLBACK = 7;
+
+// ---------------------------------------------------------------- vectors
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 v3(const LyapVec &v) { return V3{v.x, v.y, v.z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ V3 operator/(V3 a, float s) { return V3{a.x / s, a.y / s, a.z / s}; }
+// dot in the reference's order: (x*x' + y*y') + z*z'
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+// vec3.hpp:127-154: zero below 1e-12, unchanged when |v|^2 == 1, else v/|v|
+__device__ __forceinline__ V3 normalized(V3 a)
+{
+    float mag2 = a.x * a.x + a.y * a.y + a.z * a.z;
+    if ((double)mag2 < 1e-12) return v3(0.f, 0.f, 0.f);
+    if (mag2 == 1.0f || ((double)mag2 > (1.0 - 1e-12) && (double)mag2 < (1.0 + 1e-12))) return a;
+    return a / sqrtf(mag2);
+}
+
+struct C4 {
+    float x, y, z, w;
+};
+__device__ __forceinline__ C4 c4(const LyapColor &c) { return C4{c.x, c.y, c.z, c.w}; }
+__device__ __forceinline__ C4 operator+(C4 a, C4 b) { return C4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+__device__ __forceinline__ C4 operator*(C4 a, float s) { return C4{a.x * s, a.y * s, a.z * s, a.w * s}; }
+
+// VEC3::clamp(T) (vec3.hpp:190): value-preserving, the compare is in double
+__device__ __forceinline__ float clamp01(float v) { return (double)v < 0.0 ? 0.0f : ((double)v > 1.0 ? 1.0f : v); }
+
+__device__ __forceinline__ float lg2_approx(float x)
+{
+    float y;
+    asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// --------------------------------------------------------------- sequence
+// Everything the lambda loop needs about the forcing sequence, uniform per
+// warp.  `wS` packs the symbols of period positions 0..L-1 (2 bits each),
+// `wA` those of positions S..S+L-1 (mod L), where accumulation starts.
+struct SeqInfo {
+    const int32_t *seq;   // -1 terminated, device memory
+    uint32_t L;           // period (entries before the terminator)
+    uint32_t S, A;        // settle / accumulate iteration counts
+    uint32_t wS, wA;      // packed symbols when L <= 16
+    uint32_t oA;          // S mod L
+    float d;              // value of symbol D
+};
+
+__device__ __forceinline__ SeqInfo seq_setup(const int32_t *seq, uint32_t L, const LyapParams &prm)
+{
+    SeqInfo si;
+    si.seq = seq;
+    si.L = L;
+    si.S = prm.settle;
+    si.A = prm.accum;
+    si.d = prm.d;
+    si.oA = prm.settle % L;
+    si.wS = si.wA = 0;
+    if (L <= 16) {
+        uint32_t k = si.oA;
+        for (uint32_t j = 0; j < L; j++) {
+            si.wS |= ((uint32_t)seq[j] & 3u) << (2 * j);
+            si.wA |= ((uint32_t)seq[k] & 3u) << (2 * j);
+            k = (k + 1 == L) ? 0 : k + 1;
+        }
+    }
+    return si;
+}
+
+// abcd[sym] (kernel.cu:110-114), as selects on a uniform symbol
+__device__ __forceinline__ float pick(uint32_t sym, float x, float y, float z, float d)
+{
+    float lo = (sym & 1u) ? y : x;
+    float hi = (sym & 1u) ? d : z;
+    return (sym & 2u) ? hi : lo;
+}
+
+// ---------------------------------------------------------------- lambda
+// One settle step and one accumulate step of the map (kernel.cu:135,143-146).
+__device__ __forceinline__ float map_step(float r, float v)
+{
+    float t = r * v;
+    return __fmaf_rn(-t, v, t);
+}
+
+// Block end of the product form: move the float exponent of p into e, put p
+// back into [1, 2); flag a block that ended outside [2^-100, 2^100] (an
+// intermediate product may have left the normal range) or non-finite.
+__device__ __forceinline__ void renorm(float &p, int32_t &e, uint32_t &bad)
+{
+    uint32_t bits = __float_as_uint(p);
+    uint32_t ef = (bits >> 23) & 0xffu;
+    bad |= (uint32_t)((ef - 27u) > 200u);
+    e += (int32_t)ef;
+    p = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+}
+
+constexpr int ctz_lcm8(int L) { return (L % 8 == 0) ? L : (L % 4 == 0) ? 2 * L : (L % 2 == 0) ? 4 * L : 8 * L; }
+template <int L>
+struct Unroll {
+    static constexpr int U = ctz_lcm8(L) < 16 ? 16 : ctz_lcm8(L);   // multiple of L and of 8
+};
+
+// lambda for a period L <= 16: whole blocks of U = lcm(L, 8) steps run fully
+// unrolled with r in registers; the < U remaining steps run rolled, taking
+// their symbol from the packed word.  Returns lambda; `skipped` = the settle
+// landed exactly on 0.5 (or NaN) so nothing was accumulated (kernel.cu:138);
+// `fallback` = the product form had to redo the sample in the plain form.
+template <uint32_t MODE, int L>
+__device__ __forceinline__ float lambda_fixed(float x, float y, float z, const SeqInfo &si, bool &skipped,
+                                              bool &fallback)
+{
+    constexpr int U = Unroll<L>::U;
+    const float d = si.d;
+    float rS[L], rA[L], mA[L];
+#pragma unroll
+    for (int j = 0; j < L; j++) {
+        rS[j] = pick((si.wS >> (2 * j)) & 3u, x, y, z, d);
+        rA[j] = pick((si.wA >> (2 * j)) & 3u, x, y, z, d);
+        mA[j] = -2.0f * rA[j];
+    }
+    float v = 0.5f;
+    const uint32_t S = si.S, A = si.A;
+    {
+        const uint32_t nb = S / U, rem = S - nb * U;
+        for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+            for (int j = 0; j < U; j++) v = map_step(rS[j % L], v);
+        }
+        uint32_t k = 0;
+        for (uint32_t j = 0; j < rem; j++) {
+            v = map_step(pick((si.wS >> (2 * k)) & 3u, x, y, z, d), v);
+            k = (k + 1 == (uint32_t)L) ? 0 : k + 1;
+        }
+    }
+    skipped = !(v < 0.5f || v > 0.5f);
+    fallback = false;
+    float l2 = 0.0f;
+    if (!skipped) {
+        const uint32_t nb = A / U, rem = A - nb * U;
+        if (MODE == MODE_PLAIN) {
+            for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+                for (int j = 0; j < U; j++) {
+                    v = map_step(rA[j % L], v);
+                    float dd = __fmaf_rn(mA[j % L], v, rA[j % L]);
+                    l2 += lg2_approx(fabsf(dd));
+                }
+            }
+            uint32_t k = 0;
+            for (uint32_t j = 0; j < rem; j++) {
+                const float r = pick((si.wA >> (2 * k)) & 3u, x, y, z, d);
+                k = (k + 1 == (uint32_t)L) ? 0 : k + 1;
+                v = map_step(r, v);
+                float dd = __fmaf_rn(-2.0f * r, v, r);
+                l2 += lg2_approx(fabsf(dd));
+            }
+        } else {
+            float p = 1.0f;
+            int32_t e = 0;
+            uint32_t bad = 0;
+            for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+                for (int j = 0; j < U; j++) {
+                    v = map_step(rA[j % L], v);
+                    float dd = __fmaf_rn(mA[j % L], v, rA[j % L]);
+                    p = p * fabsf(dd);
+                    if ((j & 7) == 7) renorm(p, e, bad);
+                }
+            }
+            uint32_t k = 0;
+            for (uint32_t j = 0; j < rem; j++) {
+                const float r = pick((si.wA >> (2 * k)) & 3u, x, y, z, d);
+                k = (k + 1 == (uint32_t)L) ? 0 : k + 1;
+                v = map_step(r, v);
+                float dd = __fmaf_rn(-2.0f * r, v, r);
+                p = p * fabsf(dd);
+                if ((j & 7u) == 7u) renorm(p, e, bad);
+            }
+            renorm(p, e, bad);
+            // e holds the sum of biased exponents, one bias of 127 per renorm
+            const uint32_t nrenorm = A / 8 + 1;
+            l2 = (float)(e - (int32_t)(127u * nrenorm)) + lg2_approx(p);
+            if (bad) {
+                // an intermediate product may have been subnormal: redo in the plain form
+                fallback = true;
+                bool sk, fb;
+                return lambda_fixed<MODE_PLAIN, L>(x, y, z, si, sk, fb);
+            }
+        }
+    }
+    if (!isfinite(l2)) return __int_as_float(0x7fffffff);
+    return (l2 * LN2F) / (float)A;
+}
+
+// lambda for any period: the symbol is loaded each step (uniform, L1-resident).
+template <uint32_t MODE>
+__device__ __noinline__ float lambda_generic(float x, float y, float z, const SeqInfo &si, bool &skipped,
+                                             bool &fallback)
+{
+    const float d = si.d;
+    const int32_t *seq = si.seq;
+    const uint32_t L = si.L;
+    float v = 0.5f;
+    uint32_t k = 0;
+    for (uint32_t n = 0; n < si.S; n++) {
+        float r = pick((uint32_t)seq[k] & 3u, x, y, z, d);
+        k = (k + 1 == L) ? 0 : k + 1;
+        v = map_step(r, v);
+    }
+    skipped = !(v < 0.5f || v > 0.5f);
+    fallback = false;
+    float l2 = 0.0f;
+    if (!skipped) {
+        const uint32_t kA = k;
+        const float vA = v;
+        float p = 1.0f;
+        int32_t e = 0;
+        uint32_t bad = 0;
+        for (uint32_t n = 0; n < si.A; n++) {
+            float r = pick((uint32_t)seq[k] & 3u, x, y, z, d);
+            k = (k + 1 == L) ? 0 : k + 1;
+            v = map_step(r, v);
+            float dd = __fmaf_rn(-2.0f * r, v, r);
+            if (MODE == MODE_PLAIN) {
+                l2 += lg2_approx(fabsf(dd));
+            } else {
+                p = p * fabsf(dd);
+                if ((n & 7u) == 7u) renorm(p, e, bad);
+            }
+        }
+        if (MODE == MODE_PRODUCT) {
+            renorm(p, e, bad);
+            const uint32_t nrenorm = si.A / 8 + 1;
+            l2 = (float)(e - (int32_t)(127u * nrenorm)) + lg2_approx(p);
+            if (bad) {
+                fallback = true;
+                l2 = 0.0f;
+                v = vA;
+                k = kA;
+                for (uint32_t n = 0; n < si.A; n++) {
+                    float r = pick((uint32_t)seq[k] & 3u, x, y, z, d);
+                    k = (k + 1 == L) ? 0 : k + 1;
+                    v = map_step(r, v);
+                    float dd = __fmaf_rn(-2.0f * r, v, r);
+                    l2 += lg2_approx(fabsf(dd));
+                }
+            }
+        }
+    }
+    if (!isfinite(l2)) return __int_as_float(0x7fffffff);
+    return (l2 * LN2F) / (float)si.A;
+}
+
+template <uint32_t MODE>
+__device__ __forceinline__ float eval_lambda(float x, float y, float z, const SeqInfo &si, bool &skipped,
+                                             bool &fallback)
+{
+    switch (si.L) {
+#define LYAP_CASE(n) \
+    case n: return lambda_fixed<MODE, n>(x, y, z, si, skipped, fallback);
+        LYAP_CASE(1) LYAP_CASE(2) LYAP_CASE(3) LYAP_CASE(4) LYAP_CASE(5) LYAP_CASE(6) LYAP_CASE(7) LYAP_CASE(8)
+        LYAP_CASE(9) LYAP_CASE(10) LYAP_CASE(11) LYAP_CASE(12) LYAP_CASE(13) LYAP_CASE(14) LYAP_CASE(15)
+        LYAP_CASE(16)
+#undef LYAP_CASE
+    default: return lambda_generic<MODE>(x, y, z, si, skipped, fallback);
+    }
+}
+
+// --------------------------------------------------------------- the ray
+enum : uint32_t { PH_MARCH0 = 0, PH_MARCH = 1, PH_HONE = 2, PH_NORM0 = 3 };
+
+struct Ray {
+    V3 P, V, QdV, N;
+    float t, t1, dt, Fdt, Ndt, a, c, l;
+    float Qdt, Qt0, Qt1, minQdt, mag, lprev;
+    uint32_t phase, nm, nh, cap;
+    bool near, sign;
+};
+
+struct CamRays {   // the per-frame camera quantities raymarch reads
+    V3 C, S0, SDX, SDY;
+    float M;
+};
+
+__device__ __forceinline__ CamRays cam_rays(const LyapCam &cam)
+{
+    return CamRays{v3(cam.C), v3(cam.S0), v3(cam.SDX), v3(cam.SDY), cam.M};
+}
+
+// Ray setup and box clipping (kernel.cu:160-315).  Returns false when the
+// ray misses the box [lMin, lMax]^3 (raymarch returns 1 before any sample).
+__device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapParams &prm, uint32_t sx, uint32_t sy)
+{
+    V3 V = (cam.S0 + cam.SDX * (float)sx) + cam.SDY * (float)sy;
+    V = normalized(V);
+    V = V / cam.M;
+    const double LMIN = (double)prm.lMin, LMAX = (double)prm.lMax;
+    const float INF = __int_as_float(0x7f800000), QNAN = __int_as_float(0x7fffffff);
+    float ts[6];
+    ts[0] = (V.x != 0.0f) ? (float)((LMIN - (double)cam.C.x) / (double)V.x) : INF;
+    ts[1] = (V.x != 0.0f) ? (float)((LMAX - (double)cam.C.x) / (double)V.x) : INF;
+    ts[2] = (V.y != 0.0f) ? (float)((LMIN - (double)cam.C.y) / (double)V.y) : INF;
+    ts[3] = (V.y != 0.0f) ? (float)((LMAX - (double)cam.C.y) / (double)V.y) : INF;
+    ts[4] = (V.z != 0.0f) ? (float)((LMIN - (double)cam.C.z) / (double)V.z) : INF;
+    ts[5] = (V.z != 0.0f) ? (float)((LMAX - (double)cam.C.z) / (double)V.z) : INF;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        if (ts[k] != INF) {
+            V3 P = cam.C + V * ts[k];
+            float u = (k < 2) ? P.y : P.x;
+            float w = (k < 4) ? P.z : P.y;
+            if ((double)u < LMIN || (double)u > LMAX || (double)w < LMIN || (double)w > LMAX) ts[k] = QNAN;
+        }
+    }
+    int i0 = -1, i1 = -1;
+    float t0 = 3.40282347e+38f, t1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        if (isfinite(ts[k])) {
+            if (i0 == -1 || ts[k] < t0) { t0 = ts[k]; i0 = k; }
+            if (i1 == -1 || ts[k] > t1) { t1 = ts[k]; i1 = k; }
+        }
+    }
+    if (i0 == -1 && i1 == -1) return false;
+    if (i1 == -1 || i0 == i1) {
+        t1 = t0;
+        t0 = 0.0f;
+    }
+    if (t0 < 0.0f) t0 = 0.0f;
+
+    r.V = V;
+    r.t = t0;
+    r.t1 = t1;
+    r.P = cam.C + V * t0;
+    r.a = 0.0f;
+    r.c = 0.0f;
+    float Fdt;
+    if (prm.stepMethod == 1)
+        Fdt = (t1 - t0) / prm.depth;
+    else
+        Fdt = sqrtf(V.x * V.x + V.y * V.y + V.z * V.z) / prm.depth;
+    r.Fdt = Fdt;
+    r.dt = Fdt;
+    r.Ndt = Fdt / prm.nearMultiplier;
+    r.near = false;
+    float dmin = Fdt < r.Ndt ? Fdt : r.Ndt;
+    double capd = ceil((double)(t1 - t0) / (double)dmin * 1.001) + 16.0;
+    r.cap = (capd > 0.0 && capd < (double)MARCH_MAX) ? (uint32_t)capd : MARCH_MAX;
+    r.nm = 0;
+    r.nh = 0;
+    r.phase = PH_MARCH0;
+    r.l = 0.0f;
+    return true;
+}
+
+// Where the next lambda sample of this ray is taken.
+__device__ __forceinline__ V3 ray_sample_point(const Ray &r)
+{
+    V3 Q = r.P;
+    if (r.phase >= PH_NORM0) {
+        const uint32_t k = r.phase - PH_NORM0;   // kernel.cu:457-463
+        const float m = r.mag;
+        if (k == 0) Q.x = Q.x - m;
+        else if (k == 1) Q.x = Q.x + m;
+        else if (k == 2) Q.y = Q.y - m;
+        else if (k == 3) Q.y = Q.y + m;
+        else if (k == 4) Q.z = Q.z - m;
+        else Q.z = Q.z + m;
+    }
+    return Q;
+}
+
+enum : int { RAY_CONTINUE = 0, RAY_HIT = 1, RAY_MISS = 2 };
+
+// Feed one lambda sample to the ray (kernel.cu:318-473); the ray either asks
+// for its next sample (RAY_CONTINUE) or ends.
+__device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &prm)
+{
+    const float opaque = prm.opaqueThreshold;
+    bool to_normal = false;
+    if (r.phase >= PH_NORM0) {
+        const uint32_t k = r.phase - PH_NORM0;
+        if ((k & 1u) == 0) {
+            r.lprev = lam;
+        } else {
+            const float diff = lam - r.lprev;   // ls[2i+1] - ls[2i]
+            if (k == 1) r.N.x = diff;
+            else if (k == 3) r.N.y = diff;
+            else r.N.z = diff;
+        }
+        if (k == 5) {
+            r.N = normalized(r.N);
+            return RAY_HIT;
+        }
+        r.phase += 1;
+        return RAY_CONTINUE;
+    }
+    if (r.phase == PH_HONE) {
+        r.nh += 1;
+        r.l = lam;
+        if (lam == opaque) {
+            to_normal = true;
+        } else {
+            const bool osign = r.sign;
+            r.sign = !(lam < opaque);
+            if (r.sign != osign) {
+                r.Qdt = r.Qdt * -0.5f;
+                r.QdV = r.QdV * -0.5f;
+            }
+        }
+    } else {
+        r.nm += 1;
+        r.l = lam;
+        if (r.phase == PH_MARCH) {
+            if (lam > prm.chaosThreshold) r.c = r.c + lam;
+            else if (lam > opaque) r.a = r.a + lam;
+            if (lam <= prm.nearThreshold && !r.near) {
+                r.near = true;
+                r.dt = r.Ndt;
+            } else if (lam > prm.nearThreshold && r.near) {
+                r.near = false;
+                r.dt = r.Fdt;
+            }
+        }
+        if (r.l > opaque) {
+            // march on (kernel.cu:326-363)
+            if (r.nm >= r.cap) return RAY_MISS;
+            float step = r.dt;
+            if ((double)prm.jitter != 0.0) {
+                float jit = r.l - truncf(r.l);
+                if (jit < 0.0f)
+                    jit = (float)(1.0 - (double)(jit * prm.jitter));
+                else
+                    jit = (float)(1.0 + (double)(jit * prm.jitter));
+                if (isfinite(jit)) step = r.dt * jit;
+            }
+            r.t = r.t + step;
+            r.P = r.P + r.V * step;
+            if (r.t > r.t1) return RAY_MISS;
+            r.phase = PH_MARCH;
+            return RAY_CONTINUE;
+        }
+        if (r.t > r.t1) return RAY_MISS;
+        // start honing (kernel.cu:402-416)
+        r.sign = false;
+        r.Qdt = r.dt * -0.5f;
+        r.QdV = r.V * r.Qdt;
+        r.Qt1 = r.t;
+        r.Qt0 = r.t - r.dt;
+        r.minQdt = r.dt / prm.refine;
+    }
+    if (!to_normal) {
+        // honing condition (kernel.cu:420)
+        if (r.t <= r.Qt1 && r.t >= r.Qt0 && (r.Qdt <= -r.minQdt || r.Qdt >= r.minQdt) && r.nh < HONE_CAP) {
+            r.t = r.t + r.Qdt;
+            r.P = r.P + r.QdV;
+            r.phase = PH_HONE;
+            return RAY_CONTINUE;
+        }
+    }
+    // normal from six central differences (kernel.cu:456)
+    r.mag = r.dt * prm.gradient;
+    r.phase = PH_NORM0;
+    return RAY_CONTINUE;
+}
+
+// --------------------------------------------------------------- shading
+__device__ __forceinline__ unsigned char to_byte(float ch)
+{
+    const double v = 255.0 * (double)ch;   // color.hpp:171-174, saturated (H6)
+    if (!(v > 0.0)) return 0;
+    if (v >= 255.0) return 255;
+    return (unsigned char)v;
+}
+
+// shade (kernel.cu:25-106) for one point with the reference's spot lights.
+__device__ __forceinline__ C4 shade_spot(const LyapPoint &pt, V3 camC, const LyapLight *lights, uint32_t n)
+{
+    C4 color{0.f, 0.f, 0.f, 0.f};
+    if (isnan(pt.a)) return color;
+    const V3 P = v3(pt.P), N = v3(pt.N);
+    const float c = pt.c;
+    for (uint32_t li = 0; li < n; li++) {
+        const LyapLight &L = lights[li];
+        C4 phong;
+        V3 camV = camC - P;
+        V3 lightV = v3(L.C) - P;
+        float lightD2 = lightV.x * lightV.x + lightV.y * lightV.y + lightV.z * lightV.z;
+        lightV = normalized(lightV);
+        float i = dot(lightV, N);
+        float j = dot(lightV, v3(L.V));
+        j = -j;
+        if (j > L.lightOuterCone) {
+            i = clamp01(i);
+            C4 diffuse = c4(L.diffuseColor) * (i * L.diffusePower);
+            V3 halfV = normalized(camV + lightV);
+            i = clamp01(dot(N, halfV));
+            i = powf(i, L.specularHardness);
+            C4 specular = c4(L.specularColor) * (i * L.specularPower);
+            phong = (specular + diffuse) * (L.lightRange / lightD2);
+            if (j < L.lightInnerCone) phong = phong * ((j - L.lightOuterCone) / (L.lightInnerCone - L.lightOuterCone));
+            phong = phong + c4(L.ambient);
+        } else {
+            phong = c4(L.ambient);
+        }
+        if ((double)c > 0.0) phong = phong + c4(L.chaosColor) * (float)(0.1125 / (double)logf(c));
+        color = color + phong;
+    }
+    return color;
+}
+
+// Directional Lambert light (an extension: the reference has spot lights
+// only): ambient + diffuseColor * diffusePower * clamp(N . -V_light), plus
+// the reference's chaos tint.
+__device__ __forceinline__ C4 shade_directional(const LyapPoint &pt, const LyapLight *lights, uint32_t n)
+{
+    C4 color{0.f, 0.f, 0.f, 0.f};
+    if (isnan(pt.a)) return color;
+    const V3 N = v3(pt.N);
+    for (uint32_t li = 0; li < n; li++) {
+        const LyapLight &L = lights[li];
+        const V3 toLight = v3(0.f, 0.f, 0.f) - v3(L.V);
+        const float i = clamp01(dot(N, toLight));
+        C4 phong = c4(L.diffuseColor) * (i * L.diffusePower) + c4(L.ambient);
+        if ((double)pt.c > 0.0) phong = phong + c4(L.chaosColor) * (float)(0.1125 / (double)logf(pt.c));
+        color = color + phong;
+    }
+    return color;
+}
+
+}  // namespace lyapgb

@@ -1,0 +1,101 @@
+"""Device-resident frames and volumes for the workloads of scenes.py.
+
+The buffers are torch CUDA tensors (torch is used for device memory and
+streams only); every computation goes through the C ABI (capi.py).
+"""
+import numpy as np
+
+from . import capi
+from .types import POINT_DTYPE
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class DeviceFrame:
+    """One RenderWorkload on the GPU: prepared camera/lights, device inputs and outputs."""
+
+    def __init__(self, wl, device="cuda", counts=False, stats=True):
+        torch = _torch()
+        self.wl = wl
+        self.width, self.height = wl.width, wl.height
+        self.cam = capi.cam_recalculate(wl.cam, wl.width, wl.height, 1)
+        self.lights = capi.lights_recalculate(wl.lights)
+        self.seq = capi.seq_parse(wl.seq)
+        self.prm = wl.params
+        self.light_model = wl.light_model
+        n = self.width * self.height
+        self.d_seq = torch.from_numpy(self.seq).to(device)
+        self.d_lights = torch.from_numpy(capi.lights_array(self.lights)).to(device)
+        self.d_rgba = torch.empty(n * 4, dtype=torch.uint8, device=device)
+        self.d_points = torch.empty(n * 9, dtype=torch.float32, device=device)
+        self.d_counts = torch.zeros(n * 3, dtype=torch.int32, device=device) if counts else None
+        self.d_stats = torch.zeros(capi.STAT_COUNT, dtype=torch.int64, device=device) if stats else None
+
+    def ext(self, variant=capi.VARIANT_PLAIN, **kw):
+        return capi.LyapRenderExt(variant=variant, light_model=self.light_model,
+                                  d_counts=self.d_counts.data_ptr() if self.d_counts is not None else None,
+                                  d_stats=self.d_stats.data_ptr() if self.d_stats is not None else None, **kw)
+
+    def run(self, variant=capi.VARIANT_PLAIN, stream=None, **kw):
+        capi.render(self.cam, self.prm, self.d_seq, self.seq.size, self.d_lights, len(self.lights), self.d_rgba,
+                    self.d_points, self.width, self.height, ext=self.ext(variant, **kw), stream=stream)
+
+    def reset_stats(self):
+        if self.d_stats is not None:
+            self.d_stats.zero_()
+
+    def stats(self):
+        return self.d_stats.cpu().numpy().astype(np.int64) if self.d_stats is not None else None
+
+    def iterations(self, stats=None):
+        """Logistic-map iterations the plain method performs for the recorded samples."""
+        s = self.stats() if stats is None else stats
+        return int(s[capi.STAT_SAMPLES]) * (self.prm.settle + self.prm.accum) - int(s[capi.STAT_SKIPPED]) * self.prm.accum
+
+    def rgba(self):
+        return self.d_rgba.cpu().numpy().reshape(self.height, self.width, 4)
+
+    def points(self):
+        return self.d_points.cpu().numpy().view(POINT_DTYPE).reshape(self.height, self.width)
+
+    def counts(self):
+        return self.d_counts.cpu().numpy().reshape(self.height, self.width, 3).astype(np.uint32)
+
+
+class DeviceVolume:
+    """One VolumeWorkload on the GPU."""
+
+    def __init__(self, wl, device="cuda", stats=True):
+        torch = _torch()
+        self.wl = wl
+        self.nx, self.ny, self.nz = wl.n
+        self.seq = capi.seq_parse(wl.seq)
+        self.prm = wl.params
+        self.d_seq = torch.from_numpy(self.seq).to(device)
+        self.d_out = torch.empty(self.nx * self.ny * self.nz, dtype=torch.float32, device=device)
+        self.d_stats = torch.zeros(capi.STAT_COUNT, dtype=torch.int64, device=device) if stats else None
+
+    def ext(self, variant=capi.VARIANT_PLAIN, **kw):
+        return capi.LyapVolumeExt(variant=variant,
+                                  d_stats=self.d_stats.data_ptr() if self.d_stats is not None else None, **kw)
+
+    def run(self, variant=capi.VARIANT_PLAIN, stream=None, **kw):
+        capi.volume(self.d_out, self.nx, self.ny, self.nz, self.wl.lo, self.wl.hi, self.prm, self.d_seq,
+                    self.seq.size, ext=self.ext(variant, **kw), stream=stream)
+
+    def reset_stats(self):
+        if self.d_stats is not None:
+            self.d_stats.zero_()
+
+    def stats(self):
+        return self.d_stats.cpu().numpy().astype(np.int64) if self.d_stats is not None else None
+
+    def iterations(self, stats=None):
+        s = self.stats() if stats is None else stats
+        return int(s[capi.STAT_SAMPLES]) * (self.prm.settle + self.prm.accum) - int(s[capi.STAT_SKIPPED]) * self.prm.accum
+
+    def values(self):
+        return self.d_out.cpu().numpy().reshape(self.nz, self.ny, self.nx)

@@ -169,16 +169,21 @@ def small_volume(n=64):
 
 
 def full_render(seed=1, width=1920, height=1080):
-    """1920x1080, 512 steps per ray (method 1), seeded 12-symbol sequence over
-    {A, B, C}, 200 + 1000 iterations over [2, 4]^3, camera uniform on S^3 at
-    distance 5-8 from the cube centre, one directional light."""
+    """1920x1080, 512 uniform steps per ray (method 1, no jitter), seeded
+    12-symbol sequence over {A, B, C}, 200 + 1000 iterations over [2, 4]^3,
+    camera uniform on S^3 at distance 5-8 from the cube centre, one
+    directional light.  Thresholds, honing and gradient are the reference's
+    params_init defaults (opaque -0.75, chaos -0.5, near -1, refine 32,
+    gradient 0.01; params.cu:23-36): with the surface at lambda <= -0.75 a
+    ray crosses the weakly stable shell before it stops, ~140 samples per
+    ray inside the box for seed 1."""
     rng = SplitMix64(0x4C594150_00000000 | seed)
     seq = random_sequence(rng, 12)
     q = uniform_quaternion(rng)
     dist = rng.uniform(5.0, 8.0)
     cam = orbit_camera(q, (3.0, 3.0, 3.0), dist)
-    prm = make_params(200, 1000, step_method=1, depth=512.0, opaque=0.0, near_mul=1.0,
-                      jitter=0.0, refine=1.0, gradient=0.01, lmin=2.0, lmax=4.0)
+    prm = make_params(200, 1000, step_method=1, depth=512.0, opaque=-0.75, near=-1.0, near_mul=1.0,
+                      chaos=-0.5, jitter=0.0, refine=32.0, gradient=0.01, lmin=2.0, lmax=4.0)
     light = headlight(cam, ambient=(0.08, 0.08, 0.08, 1.0))
     lq = uniform_quaternion(rng)
     light.Q.x, light.Q.y, light.Q.z, light.Q.w = lq

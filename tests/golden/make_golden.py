@@ -164,6 +164,14 @@ def main():
     out["vol32_f32"] = R32.volume(32, vp, seq)
     out["vol32_f64"] = R64.volume(32, params_to_double(vp), seq)
 
+    # the reference's kernel entry points as its own kernel.cu exports them
+    # (nvcc on the reference source; only the symbol table is read)
+    obj = os.path.join(ROOT, "oracle", "_ref", "kernel_ref.o")
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-c", os.path.join(ref_dir, "kernel.cu"),
+                    "-o", obj, f"-I{ref_dir}", "-w"], check=True, capture_output=True)
+    nm = subprocess.run(["nm", obj], check=True, capture_output=True, text=True).stdout.split("\n")
+    meta["ref_kernel_symbols"] = sorted(l.split()[-1] for l in nm if " T _Z18kernel_calc_" in l)
+
     np.savez_compressed(os.path.join(HERE, "golden_reference.npz"), **out)
     with open(os.path.join(HERE, "golden_reference.json"), "w") as f:
         json.dump(meta, f, indent=1)

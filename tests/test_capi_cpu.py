@@ -1,0 +1,171 @@
+"""The C-ABI library without a GPU: it loads, exports every symbol the public
+headers declare (and the reference's kernel entry points under the
+reference's mangled names), its host scene helpers are bit-exact against the
+reference's own host build, and argument errors come back as status codes."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+capi = pytest.importorskip("lyapunov3d_gb300.capi", reason="library not built")
+from lyapunov3d_gb300.types import LyapCam, LyapLight, LyapParams, struct_from_bytes  # noqa: E402
+
+
+def _declared_functions():
+    src = open(os.path.join(ROOT, "include", "lyap_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(lyap_[a-z0-9_]+)\s*\(", src)))
+
+
+def _exported():
+    out = subprocess.run(["nm", "-D", "--defined-only", capi.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    return {l.split()[-1] for l in out.splitlines() if " T " in l}
+
+
+def test_every_declared_symbol_is_exported():
+    decl = _declared_functions()
+    assert decl, "no declarations parsed"
+    exported = _exported()
+    missing = [d for d in decl if d not in exported]
+    assert not missing, missing
+    assert sorted(decl) == sorted(capi.EXPORTED)
+
+
+def test_reference_kernel_symbols_exported(golden):
+    meta, _ = golden
+    exported = _exported()
+    for sym in meta["ref_kernel_symbols"]:
+        assert sym in exported, sym
+
+
+def test_version_and_status_strings():
+    assert "sm_103a" in capi.version()
+    assert capi.lib.lyap_abi_version() == 1
+    assert capi.lib.lyap_status_string(capi.LYAP_ERR_SEQUENCE).decode() == "bad sequence"
+
+
+def test_seq_parse_matches_reference(golden):
+    meta, _ = golden
+    for s, expect in meta["seq"].items():
+        assert capi.seq_parse(s).tolist() == expect, s
+
+
+@pytest.mark.parametrize("bad", ["", "0", "AX", "A0", " A", "E", "a-b"])
+def test_seq_parse_rejects_what_the_reference_exits_on(bad):
+    with pytest.raises(capi.LyapError) as e:
+        capi.seq_parse(bad)
+    assert e.value.code == capi.LYAP_ERR_SEQUENCE
+
+
+def test_seq_parse_capacity():
+    with pytest.raises(capi.LyapError) as e:
+        capi.seq_parse("A9", cap=5)
+    assert e.value.code == capi.LYAP_ERR_CAPACITY
+    assert capi.seq_parse("A9", cap=11).tolist() == [0] * 10 + [-1]
+
+
+def test_cam_lights_recalculate_bit_exact(golden):
+    _, g = golden
+    for i in range(g["cams_in"].shape[0]):
+        cam = struct_from_bytes(LyapCam, g["cams_in"][i].tobytes())
+        tw, th, td = (int(x) for x in g["cams_dims"][i])
+        assert bytes(capi.cam_recalculate(cam, tw, th, td)) == g["cams_out"][i].tobytes(), i
+    lights = [struct_from_bytes(LyapLight, r.tobytes()) for r in g["lights_in"]]
+    assert [bytes(l) for l in capi.lights_recalculate(lights)] == [r.tobytes() for r in g["lights_out"]]
+
+
+def test_cam_recalculate_rejects_zero_denominator():
+    cam = LyapCam()
+    cam.Q.w = 1.0
+    with pytest.raises(capi.LyapError) as e:
+        capi.cam_recalculate(cam, 64, 64, 0)
+    assert e.value.code == capi.LYAP_ERR_INVALID_ARG
+
+
+def _render_args(**over):
+    cam, prm = LyapCam(), LyapParams()
+    a = dict(cam=ctypes.byref(cam), prm=ctypes.byref(prm), seq=ctypes.c_void_p(0x1000), seq_len=3,
+             lights=ctypes.c_void_p(0x2000), n_lights=1, rgba=ctypes.c_void_p(0x3000),
+             points=ctypes.c_void_p(0x4000), w=8, h=8, ext=None, stream=None)
+    a.update(over)
+    return a, (cam, prm)
+
+
+@pytest.mark.parametrize("over,code", [
+    (dict(cam=None), capi.LYAP_ERR_INVALID_ARG),
+    (dict(prm=None), capi.LYAP_ERR_INVALID_ARG),
+    (dict(seq=None), capi.LYAP_ERR_INVALID_ARG),
+    (dict(seq_len=1), capi.LYAP_ERR_SEQUENCE),
+    (dict(seq_len=5000), capi.LYAP_ERR_SEQUENCE),
+    (dict(lights=None), capi.LYAP_ERR_INVALID_ARG),
+    (dict(n_lights=17), capi.LYAP_ERR_INVALID_ARG),
+    (dict(rgba=None), capi.LYAP_ERR_INVALID_ARG),
+    (dict(points=None), capi.LYAP_ERR_INVALID_ARG),
+    (dict(w=0), capi.LYAP_ERR_INVALID_ARG),
+    (dict(w=65536, h=65536), capi.LYAP_ERR_INVALID_ARG),
+])
+def test_render_argument_errors(over, code):
+    a, keep = _render_args(**over)
+    rc = capi.lib.lyap_render(a["cam"], a["prm"], a["seq"], a["seq_len"], a["lights"], a["n_lights"], a["rgba"],
+                              a["points"], a["w"], a["h"], a["ext"], a["stream"])
+    assert rc == code, capi.last_error()
+    assert capi.last_error().startswith("lyap_render")
+
+
+def test_render_ext_size_checked():
+    ext = capi.LyapRenderExt()
+    ext.size = 12
+    a, keep = _render_args(ext=ctypes.byref(ext))
+    rc = capi.lib.lyap_render(a["cam"], a["prm"], a["seq"], a["seq_len"], a["lights"], a["n_lights"], a["rgba"],
+                              a["points"], a["w"], a["h"], a["ext"], a["stream"])
+    assert rc == capi.LYAP_ERR_INVALID_ARG and "LyapRenderExt.size" in capi.last_error()
+    ext = capi.LyapRenderExt(variant=7)
+    a, keep = _render_args(ext=ctypes.byref(ext))
+    assert capi.lib.lyap_render(a["cam"], a["prm"], a["seq"], a["seq_len"], a["lights"], a["n_lights"], a["rgba"],
+                                a["points"], a["w"], a["h"], a["ext"], a["stream"]) == capi.LYAP_ERR_INVALID_ARG
+
+
+def test_volume_argument_errors():
+    prm = LyapParams()
+    L = capi.lib
+    assert L.lyap_volume(None, 4, 4, 4, None, None, ctypes.byref(prm), ctypes.c_void_p(8), 3, None, None) == \
+        capi.LYAP_ERR_INVALID_ARG
+    assert L.lyap_volume(ctypes.c_void_p(8), 0, 4, 4, None, None, ctypes.byref(prm), ctypes.c_void_p(8), 3, None,
+                         None) == capi.LYAP_ERR_INVALID_ARG
+    assert L.lyap_volume(ctypes.c_void_p(8), 4, 4, 4, None, None, ctypes.byref(prm), ctypes.c_void_p(8), 1, None,
+                         None) == capi.LYAP_ERR_SEQUENCE
+    assert L.lyap_volume(ctypes.c_void_p(8), 1 << 20, 1 << 20, 1 << 20, None, None, ctypes.byref(prm),
+                         ctypes.c_void_p(8), 3, None, None) == capi.LYAP_ERR_INVALID_ARG
+
+
+def test_host_buffer_sequence_validated():
+    """lyap_volume_host sees the sequence on the host and checks it before any device work."""
+    prm = LyapParams()
+    out = np.zeros(8, dtype=np.float32)
+    for seq, code in [([0, 1, 5, -1], capi.LYAP_ERR_SEQUENCE), ([0, 1, 2], capi.LYAP_ERR_SEQUENCE),
+                      ([-1], capi.LYAP_ERR_SEQUENCE)]:
+        s = np.array(seq, dtype=np.int32)
+        rc = capi.lib.lyap_volume_host(ctypes.c_void_p(out.ctypes.data), 2, 2, 2, None, None, ctypes.byref(prm),
+                                       ctypes.c_void_p(s.ctypes.data), s.size, None, None)
+        assert rc == code, capi.last_error()
+
+
+def test_drop_in_launcher_argument_errors():
+    cam, prm = LyapCam(), LyapParams()
+    L = capi.lib
+    assert L.lyap_kernel_calc_render(0, 1, 16, 16, ctypes.c_void_p(8), ctypes.c_void_p(8), ctypes.byref(cam),
+                                     ctypes.byref(prm), ctypes.c_void_p(8), ctypes.c_void_p(8), 1, None) == \
+        capi.LYAP_ERR_INVALID_ARG
+    assert L.lyap_kernel_calc_render(1, 1, 64, 64, ctypes.c_void_p(8), ctypes.c_void_p(8), ctypes.byref(cam),
+                                     ctypes.byref(prm), ctypes.c_void_p(8), ctypes.c_void_p(8), 1, None) == \
+        capi.LYAP_ERR_INVALID_ARG
+    g = (ctypes.c_uint32 * 3)(1, 1, 0)
+    b = (ctypes.c_uint32 * 3)(8, 8, 8)
+    assert L.lyap_kernel_calc_volume(g, b, ctypes.c_void_p(8), ctypes.byref(prm), ctypes.c_void_p(8), None) == \
+        capi.LYAP_ERR_INVALID_ARG
