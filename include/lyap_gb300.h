@@ -288,6 +288,27 @@ int lyap_kernel_calc_render(uint32_t grid_x, uint32_t grid_y, uint32_t block_x, 
 int lyap_kernel_calc_volume(const uint32_t grid[3], const uint32_t block[3], float *d_exps,
                             const LyapParams *prm, int32_t *d_seq, void *stream);
 
+/* lyap_render without any device allocation.  It has no counterpart in the
+ * reference (whose front-ends cudaMalloc everything up front).  For callers
+ * that cannot allocate per call: devices or drivers without stream-ordered
+ * memory pools (where lyap_render's cudaMallocAsync of its 4-byte queue
+ * counter fails), applications that own all device memory and forbid
+ * library allocations, loops that must not risk a failing or blocking
+ * allocation mid-frame.  Same arguments and results as lyap_render; the
+ * caller still passes all inputs and outputs.  The scratch is a static
+ * device array of LYAP_NOALLOC_SCRATCH_BYTES per device (held until the
+ * library is unloaded), of which a call uses 4 bytes, zeroed on `stream`
+ * before the launch; images are limited to LYAP_MAX_PIXELS (larger sizes
+ * return LYAP_ERR_INVALID_ARG).  All calls share that array: calls whose
+ * work overlaps on the GPU race and corrupt each other's images, so
+ * serialise them.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture. */
+#define LYAP_NOALLOC_SCRATCH_BYTES 256
+int lyap_render_noalloc(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
+                        const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
+                        uint32_t width, uint32_t height, const LyapRenderExt *ext, void *stream);
+
 /* Measurement support (no reference counterpart): a pipe-rate probe whose
  * launch the caller times.  kind 0 = dependent-chain-free FFMA, kind 1 =
  * lg2.approx; *ops receives the operations performed.  The rate is the

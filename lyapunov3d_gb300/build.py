@@ -24,7 +24,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "liblyap_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["lyap_render.cu", "lyap_volume.cu", "lyap_capi.cu", "lyap_probe.cu"]
+CUDA_SOURCES = ["lyap_render.cu", "lyap_volume.cu", "lyap_capi.cu", "lyap_probe.cu", "lyap_noalloc.cu"]
 CXX_SOURCES = ["lyap_scene.cpp"]
 HEADERS = ["lyap_device.cuh", "lyap_internal.h"]
 

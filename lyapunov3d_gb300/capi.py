@@ -71,7 +71,7 @@ class LyapVolumeExt(ctypes.Structure):
 EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string",
             "lyap_seq_parse", "lyap_cam_recalculate", "lyap_lights_recalculate", "lyap_render",
             "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
-            "lyap_kernel_calc_volume", "lyap_pipe_probe"]
+            "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc"]
 
 
 def _load():
@@ -92,6 +92,7 @@ def _load():
     L.lyap_volume.argtypes = [c_void_p, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p, c_void_p,
                               c_size_t, c_void_p, c_void_p]
     L.lyap_render_host.argtypes = L.lyap_render.argtypes
+    L.lyap_render_noalloc.argtypes = L.lyap_render.argtypes
     L.lyap_volume_host.argtypes = L.lyap_volume.argtypes
     L.lyap_kernel_calc_render.argtypes = [c_uint32] * 4 + [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                                            c_void_p, c_uint32, c_void_p]
@@ -173,6 +174,14 @@ def render(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width
     _check(lib.lyap_render(ctypes.byref(cam), ctypes.byref(prm), _vp(d_seq), seq_len, _vp(d_lights), n_lights,
                            _vp(d_rgba), _vp(d_points), width, height,
                            ctypes.byref(ext) if ext is not None else None, _stream(stream)))
+
+
+def render_noalloc(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext=None,
+                   stream=None):
+    """lyap_render_noalloc: lyap_render without any device allocation (shared static scratch)."""
+    _check(lib.lyap_render_noalloc(ctypes.byref(cam), ctypes.byref(prm), _vp(d_seq), seq_len, _vp(d_lights),
+                                   n_lights, _vp(d_rgba), _vp(d_points), width, height,
+                                   ctypes.byref(ext) if ext is not None else None, _stream(stream)))
 
 
 def volume(d_out, nx, ny, nz, lo, hi, prm, d_seq, seq_len, ext=None, stream=None):

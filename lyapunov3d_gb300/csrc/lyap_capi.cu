@@ -88,7 +88,7 @@ static int check_ext_volume(const LyapVolumeExt *ext, const char *fn)
     return LYAP_OK;
 }
 
-static int check_render_args(const LyapCam *cam, const LyapParams *prm, const void *seq, size_t seq_len,
+int check_render_args(const LyapCam *cam, const LyapParams *prm, const void *seq, size_t seq_len,
                              const void *lights, uint32_t n_lights, const void *rgba, const void *points,
                              uint32_t width, uint32_t height, const LyapRenderExt *ext, const char *fn)
 {
@@ -108,7 +108,7 @@ static int check_render_args(const LyapCam *cam, const LyapParams *prm, const vo
     return check_ext_render(ext, fn);
 }
 
-static RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
+RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
                           const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
                           uint32_t width, uint32_t height, const LyapRenderExt *ext)
 {

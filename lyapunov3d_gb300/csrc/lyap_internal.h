@@ -45,6 +45,14 @@ cudaError_t launch_volume(const VolumeJob &job, uint32_t mode, unsigned long lon
 // per-device SM count (cached)
 int device_sm_count();
 
+// argument checks and job assembly shared by the render entry points (lyap_capi.cu)
+int check_render_args(const LyapCam *cam, const LyapParams *prm, const void *seq, size_t seq_len,
+                      const void *lights, uint32_t n_lights, const void *rgba, const void *points,
+                      uint32_t width, uint32_t height, const LyapRenderExt *ext, const char *fn);
+RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
+                   const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
+                   uint32_t width, uint32_t height, const LyapRenderExt *ext);
+
 // error reporting (lyap_capi.cu)
 int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
