@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--volume", type=int, default=512, help="edge of the secondary volume sweep (0 = skip)")
+    ap.add_argument("--no-jit", action="store_true", help="precompiled kernels only (no run-time specialisation)")
     return ap.parse_args()
 
 
@@ -213,6 +214,7 @@ def run_ours(args):
 
     wl = scenes.full_render(args.seed, args.width, args.height)
     frame = DeviceFrame(wl, device=dev)
+    jit = not args.no_jit
     stream = torch.cuda.current_stream(dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -223,7 +225,7 @@ def run_ours(args):
     def timed_frames(variant, k, w):
         """w untimed + k timed frames; each frame timed with its own events, L2 flushed between."""
         for _ in range(w):
-            frame.run(variant, stream=stream)
+            frame.run(variant, stream=stream, jit=jit)
         torch.cuda.synchronize()
         frame.reset_stats()
         total_ms = 0.0
@@ -231,7 +233,7 @@ def run_ours(args):
         for i in range(k):
             flush.fill_(float(i))
             evs[i][0].record(stream)
-            frame.run(variant, stream=stream)
+            frame.run(variant, stream=stream, jit=jit)
             evs[i][1].record(stream)
         torch.cuda.synchronize()
         times = [a.elapsed_time(b) for a, b in evs]
@@ -277,7 +279,7 @@ def run_ours(args):
     surf_px = int((hit_c | hit_p).sum())
     agree = float(((hit_c == hit_p) | ~(hit_c | hit_p)).mean())
     surf_agree = float((hit_c & hit_p).sum() / max(1, surf_px))
-    both = hit_c & hit_p
+    both = hit_c & hit_p & np.isfinite(pts_c[:, 8]) & np.isfinite(pts_p[:, 8])
     dl = np.abs(pts_c[both, 8].astype(np.float64) - pts_p[both, 8])
     lam_diff = {"max_abs": float(dl.max()) if dl.size else 0.0, "mean_abs": float(dl.mean()) if dl.size else 0.0}
 
@@ -308,7 +310,8 @@ def run_ours(args):
         pts_h = torch.empty(npix * 9, dtype=torch.float32, pin_memory=True).numpy()
         from lyapunov3d_gb300.types import POINT_DTYPE
         pts_h = pts_h.view(POINT_DTYPE).reshape(wl.height, wl.width)
-        ext = capi.LyapRenderExt(variant=capi.VARIANT_PRODUCT, light_model=frame.light_model)
+        ext = capi.LyapRenderExt(variant=capi.VARIANT_PRODUCT, light_model=frame.light_model,
+                                 flags=capi.FLAG_NO_JIT if args.no_jit else 0)
         for _ in range(max(1, args.warmup)):
             capi.render_host(frame.cam, frame.prm, frame.seq, frame.lights, wl.width, wl.height, ext=ext,
                              stream=stream, rgba=rgba_h, points=pts_h)
@@ -337,14 +340,15 @@ def run_ours(args):
     if args.volume > 0:
         vw = scenes.full_volume(args.volume, args.seed)
         vol = DeviceVolume(vw, device=dev)
-        vol.run(capi.VARIANT_PRODUCT, stream=stream)
+        vol.run(capi.VARIANT_PRODUCT, stream=stream, jit=jit)
+        vol.run(capi.VARIANT_PLAIN, stream=stream, jit=jit)
         torch.cuda.synchronize()
         vol.reset_stats()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(2)]
         for variant, (e0, e1) in zip([capi.VARIANT_PRODUCT, capi.VARIANT_PLAIN], evs):
             flush.fill_(0.0)
             e0.record(stream)
-            vol.run(variant, stream=stream)
+            vol.run(variant, stream=stream, jit=jit)
             e1.record(stream)
         torch.cuda.synchronize()
         tp, tq = evs[0][0].elapsed_time(evs[0][1]), evs[1][0].elapsed_time(evs[1][1])
@@ -378,6 +382,12 @@ def run_ours(args):
             "iters_per_frame": iters_frame,
             "samples_per_frame": int(chosen_st[capi.STAT_SAMPLES]) // args.steps,
             "hits_per_frame": int(chosen_st[capi.STAT_HITS]) // args.steps,
+            "warp_rounds": {"lane_utilisation": float(chosen_st[capi.STAT_LANE_ROUNDS]) /
+                                                max(1.0, 32.0 * float(chosen_st[capi.STAT_ROUNDS])),
+                            "rounds_per_frame": int(chosen_st[capi.STAT_ROUNDS]) // args.steps,
+                            "max_rounds_one_warp": int(chosen_st[capi.STAT_MAX_ROUNDS]),
+                            "speculative_samples": int(chosen_st[capi.STAT_SPEC]) // args.steps,
+                            "speculative_used": int(chosen_st[capi.STAT_SPEC_USED]) // args.steps},
             "plain": {"value": plain_value, "unit": "G iters/s", "ms_per_step": t_plain / args.steps,
                       "frames_per_s": world * args.steps / (t_plain * 1e-3),
                       "roofline_frac": plain_achieved / peak_plain},
@@ -394,6 +404,7 @@ def run_ours(args):
             "volume": volume,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
+            "jit": capi.jit_info()[1].split("\n")[0] if jit else "off",
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

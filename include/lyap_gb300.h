@@ -43,6 +43,8 @@ extern "C" {
 #define LYAP_ERR_NO_DEVICE     (-4)  /* no usable sm_103 device            */
 #define LYAP_ERR_OUT_OF_MEMORY (-5)
 #define LYAP_ERR_CAPACITY      (-6)  /* output buffer too small            */
+#define LYAP_ERR_JIT           (-7)  /* run-time specialisation required
+                                        (LYAP_FLAG_REQUIRE_JIT) but unavailable */
 
 /* Longest expanded sequence (entries, including the -1 terminator). */
 #define LYAP_MAX_SEQ_LEN 4096
@@ -152,6 +154,7 @@ typedef struct {
     double a, c, l;
 } LyapPointD;
 
+#ifndef __CUDACC_RTC__   /* offsetof checks run in host compiles */
 /* Layout checks against the reference's structs (sizes and offsets as the
  * reference's own build lays them out with CUDA's vector types). */
 #if defined(__cplusplus)
@@ -176,6 +179,7 @@ LYAP_STATIC_ASSERT(offsetof(LyapCamD, chaosColor) == 352, "LyapCamD.chaosColor")
 LYAP_STATIC_ASSERT(sizeof(LyapParamsD) == 104, "LyapParamsD size");
 LYAP_STATIC_ASSERT(offsetof(LyapParamsD, nearThreshold) == 24, "LyapParamsD.nearThreshold");
 LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
+#endif /* !__CUDACC_RTC__ */
 
 /* ---- extensions (kept out of the reference structs) -------------------- */
 #define LYAP_VERSION_STRING "0.1.0"
@@ -193,7 +197,9 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_LIGHT_DIRECTIONAL 1u /* Lambert: ambient + diffuse*clamp(N.-V)  */
 
 /* Slots of the optional statistics array (LyapRenderExt / LyapVolumeExt
- * d_stats, 8 x uint64, accumulated with atomics; the caller zeroes it).
+ * d_stats, LYAP_STAT_COUNT x uint64, accumulated with atomics; the caller
+ * zeroes it).  Speculative samples that a ray does not use are not counted
+ * in SAMPLES.
  * Logistic-map iterations performed = SAMPLES*(settle+accum) - SKIPPED*accum. */
 #define LYAP_STAT_SAMPLES  0  /* lambda evaluations                          */
 #define LYAP_STAT_SKIPPED  1  /* evaluations whose settle landed on x = 0.5  */
@@ -203,18 +209,34 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_STAT_HITS     5  /* render: rays that hit                       */
 #define LYAP_STAT_RAYS     6  /* render: rays finished                       */
 #define LYAP_STAT_FALLBACK 7  /* product evaluations redone in plain form    */
-#define LYAP_STAT_COUNT    8
+#define LYAP_STAT_SPEC     8  /* render: samples taken ahead by idle lanes   */
+#define LYAP_STAT_SPEC_USED 9 /* render: of those, samples the rays used      */
+#define LYAP_STAT_ROUNDS   10 /* render: warp rounds (one lambda sample each) */
+#define LYAP_STAT_LANE_ROUNDS 11 /* render: lanes sampling, summed over rounds */
+#define LYAP_STAT_MAX_ROUNDS 12  /* render: most rounds of any warp (max)     */
+#define LYAP_STAT_COUNT    13
+
+/* LyapRenderExt / LyapVolumeExt flags.  Given the host copy of the sequence
+ * (h_seq), the library compiles the kernels for that sequence at run time
+ * (NVRTC, cached per sequence for the process; identical results, fewer
+ * registers, faster); without NVRTC or for periods above 32 it uses its
+ * precompiled kernels. */
+#define LYAP_FLAG_NO_JIT      1u  /* always use the precompiled kernels       */
+#define LYAP_FLAG_REQUIRE_JIT 2u  /* fail (LYAP_ERR_JIT) instead of falling back */
+#define LYAP_FLAG_NO_SPECULATION 4u /* render: idle lanes do not take samples
+                                       ahead for running rays (same results) */
 
 typedef struct {
     uint32_t size;               /* = sizeof(LyapRenderExt) */
     uint32_t variant;            /* LYAP_VARIANT_* (default PLAIN) */
     uint32_t light_model;        /* LYAP_LIGHT_* (default SPOT) */
-    uint32_t flags;              /* reserved, 0 */
+    uint32_t flags;              /* LYAP_FLAG_* */
     uint32_t *d_counts;          /* optional device array, 3 per pixel:
                                     march, honing, normal samples */
     unsigned long long *d_stats; /* optional device array, LYAP_STAT_COUNT */
     uint32_t blocks_per_sm;      /* launch shape, 0 = automatic */
     uint32_t threads_per_block;  /* multiple of 32, <= 128; 0 = automatic */
+    const int32_t *h_seq;        /* optional host copy of d_seq (seq_len entries) */
 } LyapRenderExt;
 
 typedef struct {
@@ -223,8 +245,12 @@ typedef struct {
     unsigned long long *d_stats; /* optional, LYAP_STAT_COUNT */
     uint32_t blocks_per_sm;      /* 0 = automatic */
     uint32_t threads_per_block;  /* multiple of 32, <= 256; 0 = automatic */
+    uint32_t flags;              /* LYAP_FLAG_* */
+    uint32_t pad_;
+    const int32_t *h_seq;        /* optional host copy of d_seq */
 } LyapVolumeExt;
 
+#ifndef __CUDACC_RTC__   /* host entry points: not part of device-side compiles */
 /* ---- entry points ------------------------------------------------------ */
 
 int lyap_abi_version(void);
@@ -309,11 +335,18 @@ int lyap_render_noalloc(const LyapCam *cam, const LyapParams *prm, const int32_t
                         const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
                         uint32_t width, uint32_t height, const LyapRenderExt *ext, void *stream);
 
+/* State of the run-time specialisation (no reference counterpart): writes a
+ * one-line description (NVRTC loaded or why not, compiles, launches, cached
+ * sequences, the last compile errors) into buf; returns 1 if NVRTC loaded. */
+int lyap_jit_info(char *buf, size_t cap);
+
 /* Measurement support (no reference counterpart): a pipe-rate probe whose
  * launch the caller times.  kind 0 = dependent-chain-free FFMA, kind 1 =
  * lg2.approx; *ops receives the operations performed.  The rate is the
  * denominator of the lambda kernels' FP32 / MUFU roofline. */
 int lyap_pipe_probe(uint32_t kind, uint32_t iters, float *d_sink, double *ops, void *stream);
+
+#endif /* !__CUDACC_RTC__ */
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -25,8 +25,22 @@ LIB = os.path.join(LIBDIR, "liblyap_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["lyap_render.cu", "lyap_volume.cu", "lyap_capi.cu", "lyap_probe.cu", "lyap_noalloc.cu"]
-CXX_SOURCES = ["lyap_scene.cpp"]
-HEADERS = ["lyap_device.cuh", "lyap_internal.h"]
+CXX_SOURCES = ["lyap_scene.cpp", "lyap_jit.cpp"]
+HEADERS = ["lyap_device.cuh", "lyap_internal.h", "lyap_jobs.h", "lyap_kernels.cuh", "lyap_jit.h"]
+# headers NVRTC compiles at run time (embedded into the library), and minimal
+# stand-ins for the two C headers they include
+JIT_HEADERS = [("lyap_gb300.h", "INCLUDE"), ("lyap_jobs.h", "CSRC"), ("lyap_device.cuh", "CSRC"),
+               ("lyap_kernels.cuh", "CSRC")]
+JIT_STUBS = {
+    "stdint.h": ("#pragma once\n"
+                 "typedef signed char int8_t; typedef short int16_t; typedef int int32_t;\n"
+                 "typedef long long int64_t; typedef unsigned char uint8_t; typedef unsigned short uint16_t;\n"
+                 "typedef unsigned int uint32_t; typedef unsigned long long uint64_t;\n"),
+    "stddef.h": ("#pragma once\n"
+                 "typedef unsigned long size_t; typedef long ptrdiff_t;\n"
+                 "#define offsetof(t, m) __builtin_offsetof(t, m)\n"
+                 "#ifndef NULL\n#define NULL 0\n#endif\n"),
+}
 
 
 def nvcc_path():
@@ -64,6 +78,30 @@ def _run(cmd, verbose):
     return r.stdout + r.stderr
 
 
+def write_jit_sources(path):
+    """A C++ file holding the JIT headers as raw string literals (lyap_jit.cpp reads them)."""
+    names, texts = [], []
+    for name, where in JIT_HEADERS:
+        with open(os.path.join(INCLUDE if where == "INCLUDE" else CSRC, name)) as f:
+            names.append(name)
+            texts.append(f.read())
+    for name, text in JIT_STUBS.items():
+        names.append(name)
+        texts.append(text)
+    out = ["// generated by lyapunov3d_gb300/build.py: device headers for run-time compilation", "namespace lyapgb {",
+           f"extern const int kJitHeaderCount = {len(names)};", "extern const char *const kJitHeaderNames[] = {"]
+    out += [f'    "{n}",' for n in names] + ["};", "extern const char *const kJitHeaderSources[] = {"]
+    for t in texts:
+        assert ")LYAPSRC\"" not in t
+        out.append('    R"LYAPSRC(' + t + ')LYAPSRC",')
+    out += ["};", "}  // namespace lyapgb", ""]
+    data = "\n".join(out)
+    if not os.path.exists(path) or open(path).read() != data:
+        with open(path, "w") as f:
+            f.write(data)
+    return path
+
+
 def build(force=False, verbose=False, ptxas_verbose=False):
     """Compile and link the library; returns its path."""
     if not force and up_to_date():
@@ -76,18 +114,20 @@ def build(force=False, verbose=False, ptxas_verbose=False):
     for f in CUDA_SOURCES:
         obj = os.path.join(OBJDIR, f + ".o")
         jobs.append([nvcc, *nvcc_flags(extra), "-c", os.path.join(CSRC, f), "-o", obj])
-    for f in CXX_SOURCES:
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include")
+    jit_src = write_jit_sources(os.path.join(OBJDIR, "lyap_jit_sources.cpp"))
+    for f in CXX_SOURCES + ["lyap_jit_sources.cpp"]:
         obj = os.path.join(OBJDIR, f + ".o")
+        src = jit_src if f == "lyap_jit_sources.cpp" else os.path.join(CSRC, f)
         jobs.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
-                     "-fno-fast-math", f"-I{INCLUDE}", f"-I{CSRC}", "-I/usr/local/cuda/include", "-c",
-                     os.path.join(CSRC, f), "-o", obj])
+                     "-fno-fast-math", f"-I{INCLUDE}", f"-I{CSRC}", f"-I{cuda_inc}", "-c", src, "-o", obj])
     logs = []
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for out in ex.map(lambda c: _run(c, verbose), jobs):
             logs.append(out)
-    objs = [os.path.join(OBJDIR, f + ".o") for f in CUDA_SOURCES + CXX_SOURCES]
+    objs = [os.path.join(OBJDIR, f + ".o") for f in CUDA_SOURCES + CXX_SOURCES + ["lyap_jit_sources.cpp"]]
     tmp = LIB + ".tmp"
-    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs], verbose)
+    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-ldl"], verbose)
     os.replace(tmp, LIB)
     if ptxas_verbose:
         print("\n".join(l for l in logs if l.strip()))

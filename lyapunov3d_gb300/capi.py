@@ -25,6 +25,10 @@ LYAP_ERR_CUDA = -3
 LYAP_ERR_NO_DEVICE = -4
 LYAP_ERR_OUT_OF_MEMORY = -5
 LYAP_ERR_CAPACITY = -6
+LYAP_ERR_JIT = -7
+FLAG_NO_JIT = 1
+FLAG_REQUIRE_JIT = 2
+FLAG_NO_SPECULATION = 4
 
 VARIANT_PLAIN = 0
 VARIANT_PRODUCT = 1
@@ -33,8 +37,9 @@ LIGHT_DIRECTIONAL = 1
 MAX_SEQ_LEN = 4096
 MAX_LIGHTS = 16
 
-STAT_SAMPLES, STAT_SKIPPED, STAT_MARCH, STAT_HONE, STAT_NORMAL, STAT_HITS, STAT_RAYS, STAT_FALLBACK = range(8)
-STAT_COUNT = 8
+(STAT_SAMPLES, STAT_SKIPPED, STAT_MARCH, STAT_HONE, STAT_NORMAL, STAT_HITS, STAT_RAYS, STAT_FALLBACK, STAT_SPEC,
+ STAT_SPEC_USED, STAT_ROUNDS, STAT_LANE_ROUNDS, STAT_MAX_ROUNDS) = range(13)
+STAT_COUNT = 13
 
 
 class LyapError(RuntimeError):
@@ -47,7 +52,7 @@ class LyapError(RuntimeError):
 class LyapRenderExt(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("variant", c_uint32), ("light_model", c_uint32), ("flags", c_uint32),
                 ("d_counts", c_void_p), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
-                ("threads_per_block", c_uint32)]
+                ("threads_per_block", c_uint32), ("h_seq", c_void_p)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -58,7 +63,7 @@ class LyapRenderExt(ctypes.Structure):
 
 class LyapVolumeExt(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("variant", c_uint32), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
-                ("threads_per_block", c_uint32)]
+                ("threads_per_block", c_uint32), ("flags", c_uint32), ("pad_", c_uint32), ("h_seq", c_void_p)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -71,7 +76,7 @@ class LyapVolumeExt(ctypes.Structure):
 EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string",
             "lyap_seq_parse", "lyap_cam_recalculate", "lyap_lights_recalculate", "lyap_render",
             "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
-            "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc"]
+            "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc", "lyap_jit_info"]
 
 
 def _load():
@@ -99,6 +104,7 @@ def _load():
     L.lyap_kernel_calc_volume.argtypes = [POINTER(c_uint32), POINTER(c_uint32), c_void_p, c_void_p, c_void_p,
                                           c_void_p]
     L.lyap_pipe_probe.argtypes = [c_uint32, c_uint32, c_void_p, POINTER(ctypes.c_double), c_void_p]
+    L.lyap_jit_info.argtypes = [ctypes.c_char_p, c_size_t]
     for name in EXPORTED:
         if name not in ("lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string"):
             getattr(L, name).restype = c_int
@@ -112,6 +118,13 @@ def _check(rc):
     if rc != LYAP_OK:
         raise LyapError(rc, lib.lyap_last_error_string().decode(errors="replace"))
     return rc
+
+
+def jit_info():
+    """(nvrtc_loaded, description) of the run-time specialisation."""
+    buf = ctypes.create_string_buffer(4096)
+    ok = lib.lyap_jit_info(buf, 4096)
+    return bool(ok), buf.value.decode(errors="replace")
 
 
 def version():

@@ -8,10 +8,12 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <string>
 
 #include "lyap_device.cuh"
 #include "lyap_gb300.h"
 #include "lyap_internal.h"
+#include "lyap_jit.h"
 
 namespace lyapgb {
 
@@ -126,6 +128,7 @@ RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_s
     job.width = width;
     job.height = height;
     job.light_model = ext ? ext->light_model : LYAP_LIGHT_SPOT;
+    job.flags = ext ? ext->flags : 0u;
     return job;
 }
 
@@ -151,6 +154,7 @@ const char *lyap_status_string(int code)
     case LYAP_ERR_NO_DEVICE: return "no usable sm_103 device";
     case LYAP_ERR_OUT_OF_MEMORY: return "out of device memory";
     case LYAP_ERR_CAPACITY: return "output buffer too small";
+    case LYAP_ERR_JIT: return "specialised kernel unavailable";
     default: return "unknown status";
     }
 }
@@ -170,9 +174,29 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     cudaError_t e = cudaMallocAsync((void **)&d_counter, sizeof(uint32_t), s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: scratch allocation");
     e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s);
-    if (e == cudaSuccess)
-        e = launch_render(job, ext ? ext->variant : LYAP_VARIANT_PLAIN, d_counter, ext ? ext->d_stats : nullptr,
-                          ext ? ext->blocks_per_sm : 0, ext ? ext->threads_per_block : 0, s);
+    if (e == cudaSuccess) {
+        const uint32_t variant = ext ? ext->variant : LYAP_VARIANT_PLAIN;
+        const uint32_t flags = ext ? ext->flags : 0u;
+        bool launched = false;
+        if (ext && ext->h_seq && !(flags & LYAP_FLAG_NO_JIT)) {
+            std::string why;
+            cudaError_t le = cudaSuccess;
+            if (jit_launch_render(job, variant, ext->h_seq, d_counter, ext->d_stats, ext->blocks_per_sm,
+                                  ext->threads_per_block, s, &le, &why)) {
+                e = le;
+                launched = true;
+            } else if (flags & LYAP_FLAG_REQUIRE_JIT) {
+                cudaFreeAsync(d_counter, s);
+                return set_error(LYAP_ERR_JIT, "lyap_render: specialised kernel unavailable: %s", why.c_str());
+            }
+        } else if (flags & LYAP_FLAG_REQUIRE_JIT) {
+            cudaFreeAsync(d_counter, s);
+            return set_error(LYAP_ERR_JIT, "lyap_render: LYAP_FLAG_REQUIRE_JIT needs ext->h_seq");
+        }
+        if (!launched)
+            e = launch_render(job, variant, d_counter, ext ? ext->d_stats : nullptr, ext ? ext->blocks_per_sm : 0,
+                              ext ? ext->threads_per_block : 0, s);
+    }
     cudaError_t e2 = cudaFreeAsync(d_counter, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: launch");
     if (e2 != cudaSuccess) return cuda_error(e2, "lyap_render: scratch release");
@@ -205,9 +229,23 @@ int lyap_volume(float *d_out, uint32_t nx, uint32_t ny, uint32_t nz, const float
         job.lo[k] = lo ? lo[k] : 0.0f;   // kernel.cu:527-529: [0, 4) when not given
         job.hi[k] = hi ? hi[k] : 4.0f;
     }
-    cudaError_t e = launch_volume(job, ext ? ext->variant : LYAP_VARIANT_PLAIN, ext ? ext->d_stats : nullptr,
-                                  ext ? ext->blocks_per_sm : 0, ext ? ext->threads_per_block : 0,
-                                  (cudaStream_t)stream);
+    const uint32_t variant = ext ? ext->variant : LYAP_VARIANT_PLAIN;
+    const uint32_t flags = ext ? ext->flags : 0u;
+    cudaError_t e = cudaSuccess;
+    bool launched = false;
+    if (ext && ext->h_seq && !(flags & LYAP_FLAG_NO_JIT)) {
+        std::string why;
+        if (jit_launch_volume(job, variant, ext->h_seq, ext->d_stats, ext->blocks_per_sm, ext->threads_per_block,
+                              (cudaStream_t)stream, &e, &why))
+            launched = true;
+        else if (flags & LYAP_FLAG_REQUIRE_JIT)
+            return set_error(LYAP_ERR_JIT, "lyap_volume: specialised kernel unavailable: %s", why.c_str());
+    } else if (flags & LYAP_FLAG_REQUIRE_JIT) {
+        return set_error(LYAP_ERR_JIT, "lyap_volume: LYAP_FLAG_REQUIRE_JIT needs ext->h_seq");
+    }
+    if (!launched)
+        e = launch_volume(job, variant, ext ? ext->d_stats : nullptr, ext ? ext->blocks_per_sm : 0,
+                          ext ? ext->threads_per_block : 0, (cudaStream_t)stream);
     if (e != cudaSuccess) return cuda_error(e, "lyap_volume: launch");
     return LYAP_OK;
 }
@@ -234,8 +272,17 @@ int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *s
     e = cudaMemcpyAsync(dev, seq, seq_b, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && light_b) e = cudaMemcpyAsync(dev + off_l, lights, light_b, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
+        // the sequence is on the host here: hand it on for the specialised kernels
+        LyapRenderExt x;
+        if (ext) {
+            x = *ext;
+        } else {
+            memset(&x, 0, sizeof(x));
+            x.size = sizeof(x);
+        }
+        if (!x.h_seq) x.h_seq = seq;
         rc = lyap_render(cam, prm, (const int32_t *)dev, seq_len, (const LyapLight *)(dev + off_l), n_lights,
-                         (RGBA *)(dev + off_r), (LyapPoint *)(dev + off_p), width, height, ext, stream);
+                         (RGBA *)(dev + off_r), (LyapPoint *)(dev + off_p), width, height, &x, stream);
         if (rc) {
             cudaFreeAsync(dev, s);
             return rc;
@@ -270,7 +317,15 @@ int lyap_volume_host(float *out, uint32_t nx, uint32_t ny, uint32_t nz, const fl
     if (e != cudaSuccess) return cuda_error(e, "lyap_volume_host: device buffers");
     e = cudaMemcpyAsync(dev + seq_off, seq, seq_len * sizeof(int32_t), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {
-        rc = lyap_volume((float *)dev, nx, ny, nz, lo, hi, prm, (const int32_t *)(dev + seq_off), seq_len, ext, stream);
+        LyapVolumeExt x;
+        if (ext) {
+            x = *ext;
+        } else {
+            memset(&x, 0, sizeof(x));
+            x.size = sizeof(x);
+        }
+        if (!x.h_seq) x.h_seq = seq;
+        rc = lyap_volume((float *)dev, nx, ny, nz, lo, hi, prm, (const int32_t *)(dev + seq_off), seq_len, &x, stream);
         if (rc) {
             cudaFreeAsync(dev, s);
             return rc;

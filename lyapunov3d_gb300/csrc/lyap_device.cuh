@@ -17,7 +17,9 @@
 //    the four candidate values of r held in registers.
 #pragma once
 
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
+#endif
 #include <stdint.h>
 
 #include "lyap_gb300.h"
@@ -34,6 +36,10 @@ constexpr float LN2F = 0.693147180559945309417232121458f;
 // statistics slots (LYAP_STAT_* in lyap_gb300.h)
 constexpr int ST_SAMPLES = 0, ST_SKIPPED = 1, ST_MARCH = 2, ST_HONE = 3, ST_NORMAL = 4,
               ST_HITS = 5, ST_RAYS = 6, ST_FALLBACK = 7;
+
+// Exact float classification without library calls (identical under nvcc and NVRTC).
+__device__ __forceinline__ bool f_isnan(float v) { return v != v; }
+__device__ __forceinline__ bool f_isfinite(float v) { return (__float_as_uint(v) & 0x7f800000u) != 0x7f800000u; }
 
 // ---------------------------------------------------------------- vectors
 struct V3 {
@@ -136,11 +142,15 @@ __device__ __forceinline__ void renorm(float &p, int32_t &e, uint32_t &bad)
     p = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
 }
 
-constexpr int ctz_lcm8(int L) { return (L % 8 == 0) ? L : (L % 4 == 0) ? 2 * L : (L % 2 == 0) ? 4 * L : 8 * L; }
+__host__ __device__ constexpr int ctz_lcm8(int L) { return (L % 8 == 0) ? L : (L % 4 == 0) ? 2 * L : (L % 2 == 0) ? 4 * L : 8 * L; }
 template <int L>
 struct Unroll {
     static constexpr int U = ctz_lcm8(L) < 16 ? 16 : ctz_lcm8(L);   // multiple of L and of 8
 };
+
+template <uint32_t MODE>
+__device__ __noinline__ float lambda_generic(float x, float y, float z, const SeqInfo &si, bool &skipped,
+                                             bool &fallback);
 
 // lambda for a period L <= 16: whole blocks of U = lcm(L, 8) steps run fully
 // unrolled with r in registers; the < U remaining steps run rolled, taking
@@ -223,14 +233,15 @@ __device__ __forceinline__ float lambda_fixed(float x, float y, float z, const S
             const uint32_t nrenorm = A / 8 + 1;
             l2 = (float)(e - (int32_t)(127u * nrenorm)) + lg2_approx(p);
             if (bad) {
-                // an intermediate product may have been subnormal: redo in the plain form
+                // an intermediate product may have been subnormal: redo in the plain
+                // form (the rolled evaluator: same operations, kept out of line)
                 fallback = true;
                 bool sk, fb;
-                return lambda_fixed<MODE_PLAIN, L>(x, y, z, si, sk, fb);
+                return lambda_generic<MODE_PLAIN>(x, y, z, si, sk, fb);
             }
         }
     }
-    if (!isfinite(l2)) return __int_as_float(0x7fffffff);
+    if (!f_isfinite(l2)) return __int_as_float(0x7fffffff);
     return (l2 * LN2F) / (float)A;
 }
 
@@ -289,7 +300,7 @@ __device__ __noinline__ float lambda_generic(float x, float y, float z, const Se
             }
         }
     }
-    if (!isfinite(l2)) return __int_as_float(0x7fffffff);
+    if (!f_isfinite(l2)) return __int_as_float(0x7fffffff);
     return (l2 * LN2F) / (float)si.A;
 }
 
@@ -305,6 +316,169 @@ __device__ __forceinline__ float eval_lambda(float x, float y, float z, const Se
         LYAP_CASE(16)
 #undef LYAP_CASE
     default: return lambda_generic<MODE>(x, y, z, si, skipped, fallback);
+    }
+}
+
+// ------------------------------------------- lambda, sequence known at compile time
+// A period of up to 64 symbols packed 2 bits each into two 64-bit template
+// constants.  When the loop below is unrolled, at(j) folds to a constant, so
+// picking r for a step is a register choice, not an instruction: the loop
+// keeps only x, y, z, d, their -2 multiples and the orbit state live, which
+// leaves room for K independent samples per thread (K dependency chains
+// interleaved to hide the 8-cycle FMUL->FFMA latency of one chain).
+template <int L_, uint64_t W0, uint64_t W1>
+struct CSeq {
+    static constexpr int L = L_;
+    __device__ static constexpr uint32_t at(int j)
+    {
+        return (uint32_t)(((j < 32) ? (W0 >> (2 * j)) : (W1 >> (2 * (j - 32)))) & 3u);
+    }
+    __device__ static __forceinline__ uint32_t at_rt(uint32_t j)
+    {
+        return (uint32_t)(((j < 32u) ? (W0 >> (2u * j)) : (W1 >> (2u * (j - 32u)))) & 3u);
+    }
+};
+
+template <int L>
+struct UnrollC {
+    static constexpr int U = (L <= 16) ? Unroll<L>::U : ((L % 8 == 0) ? L : ctz_lcm8(L) <= 256 ? ctz_lcm8(L) : L);
+    static constexpr bool aligned8 = (U % 8) == 0;   // renormalisation points fall on j % 8 == 7
+};
+
+// K samples (px[k], py[k], pz[k]) with the settle symbols SS and the
+// accumulation symbols SA (SS rotated by settle mod L).  Same arithmetic as
+// lambda_fixed, sample by sample.  skipped / fallback: bit k set for sample k.
+template <uint32_t MODE, int K, class SS, class SA>
+__device__ __forceinline__ void lambda_const(const float (&px)[K], const float (&py)[K], const float (&pz)[K],
+                                             float d, uint32_t S, uint32_t A, float (&out)[K],
+                                             uint32_t &skipped, uint32_t &fallback)
+{
+    constexpr int L = SS::L;
+    constexpr int U = UnrollC<L>::U;
+    static_assert(UnrollC<L>::aligned8 || MODE == MODE_PLAIN, "product form needs U % 8 == 0");
+    const float md = -2.0f * d;
+    float mx[K], my[K], mz[K], v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        mx[k] = -2.0f * px[k];
+        my[k] = -2.0f * py[k];
+        mz[k] = -2.0f * pz[k];
+        v[k] = 0.5f;
+    }
+    {
+        const uint32_t nb = S / U, rem = S - nb * U;
+        for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+            for (int j = 0; j < U; j++) {
+#pragma unroll
+                for (int k = 0; k < K; k++) v[k] = map_step(pick(SS::at(j % L), px[k], py[k], pz[k], d), v[k]);
+            }
+        }
+        uint32_t jj = 0;
+        for (uint32_t j = 0; j < rem; j++) {
+            const uint32_t sym = SS::at_rt(jj);
+            jj = (jj + 1 == (uint32_t)L) ? 0 : jj + 1;
+#pragma unroll
+            for (int k = 0; k < K; k++) v[k] = map_step(pick(sym, px[k], py[k], pz[k], d), v[k]);
+        }
+    }
+    skipped = 0;
+    fallback = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+        if (!(v[k] < 0.5f || v[k] > 0.5f)) skipped |= 1u << k;
+    float l2[K];
+    const uint32_t nb = A / U, rem = A - nb * U;
+    if (MODE == MODE_PLAIN) {
+#pragma unroll
+        for (int k = 0; k < K; k++) l2[k] = 0.0f;
+        for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+            for (int j = 0; j < U; j++) {
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const uint32_t sym = SA::at(j % L);
+                    const float r = pick(sym, px[k], py[k], pz[k], d);
+                    const float m = pick(sym, mx[k], my[k], mz[k], md);
+                    v[k] = map_step(r, v[k]);
+                    l2[k] += lg2_approx(fabsf(__fmaf_rn(m, v[k], r)));
+                }
+            }
+        }
+        uint32_t jj = 0;
+        for (uint32_t j = 0; j < rem; j++) {
+            const uint32_t sym = SA::at_rt(jj);
+            jj = (jj + 1 == (uint32_t)L) ? 0 : jj + 1;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float r = pick(sym, px[k], py[k], pz[k], d);
+                const float m = pick(sym, mx[k], my[k], mz[k], md);
+                v[k] = map_step(r, v[k]);
+                l2[k] += lg2_approx(fabsf(__fmaf_rn(m, v[k], r)));
+            }
+        }
+    } else {
+        float p[K];
+        int32_t e[K];
+        uint32_t bad[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            p[k] = 1.0f;
+            e[k] = 0;
+            bad[k] = 0;
+        }
+        for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+            for (int j = 0; j < U; j++) {
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const uint32_t sym = SA::at(j % L);
+                    const float r = pick(sym, px[k], py[k], pz[k], d);
+                    const float m = pick(sym, mx[k], my[k], mz[k], md);
+                    v[k] = map_step(r, v[k]);
+                    p[k] = p[k] * fabsf(__fmaf_rn(m, v[k], r));
+                    if ((j & 7) == 7) renorm(p[k], e[k], bad[k]);
+                }
+            }
+        }
+        uint32_t jj = 0;
+        for (uint32_t j = 0; j < rem; j++) {
+            const uint32_t sym = SA::at_rt(jj);
+            jj = (jj + 1 == (uint32_t)L) ? 0 : jj + 1;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const float r = pick(sym, px[k], py[k], pz[k], d);
+                const float m = pick(sym, mx[k], my[k], mz[k], md);
+                v[k] = map_step(r, v[k]);
+                p[k] = p[k] * fabsf(__fmaf_rn(m, v[k], r));
+                if ((j & 7u) == 7u) renorm(p[k], e[k], bad[k]);
+            }
+        }
+        const int32_t bias = (int32_t)(127u * (A / 8 + 1));
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            renorm(p[k], e[k], bad[k]);
+            l2[k] = (float)(e[k] - bias) + lg2_approx(p[k]);
+            if (bad[k] && !((skipped >> k) & 1u)) fallback |= 1u << k;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        float lk = ((skipped >> k) & 1u) ? 0.0f : l2[k];
+        out[k] = f_isfinite(lk) ? (lk * LN2F) / (float)A : __int_as_float(0x7fffffff);
+    }
+    if (MODE == MODE_PRODUCT && fallback) {
+        // an intermediate product may have been subnormal: redo those samples in the plain form
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if ((fallback >> k) & 1u) {
+                const float qx[1] = {px[k]}, qy[1] = {py[k]}, qz[1] = {pz[k]};
+                float o[1];
+                uint32_t sk, fb;
+                lambda_const<MODE_PLAIN, 1, SS, SA>(qx, qy, qz, d, S, A, o, sk, fb);
+                out[k] = o[0];
+            }
+        }
     }
 }
 
@@ -358,7 +532,7 @@ __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapP
     float t0 = 3.40282347e+38f, t1 = 0.0f;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        if (isfinite(ts[k])) {
+        if (f_isfinite(ts[k])) {
             if (i0 == -1 || ts[k] < t0) { t0 = ts[k]; i0 = k; }
             if (i1 == -1 || ts[k] > t1) { t1 = ts[k]; i1 = k; }
         }
@@ -468,13 +642,13 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
             // march on (kernel.cu:326-363)
             if (r.nm >= r.cap) return RAY_MISS;
             float step = r.dt;
-            if ((double)prm.jitter != 0.0) {
+            if (prm.jitter != 0.0f) {   // the reference compares in double; same outcome for a float
                 float jit = r.l - truncf(r.l);
                 if (jit < 0.0f)
                     jit = (float)(1.0 - (double)(jit * prm.jitter));
                 else
                     jit = (float)(1.0 + (double)(jit * prm.jitter));
-                if (isfinite(jit)) step = r.dt * jit;
+                if (f_isfinite(jit)) step = r.dt * jit;
             }
             r.t = r.t + step;
             r.P = r.P + r.V * step;
@@ -519,7 +693,7 @@ __device__ __forceinline__ unsigned char to_byte(float ch)
 __device__ __forceinline__ C4 shade_spot(const LyapPoint &pt, V3 camC, const LyapLight *lights, uint32_t n)
 {
     C4 color{0.f, 0.f, 0.f, 0.f};
-    if (isnan(pt.a)) return color;
+    if (f_isnan(pt.a)) return color;
     const V3 P = v3(pt.P), N = v3(pt.N);
     const float c = pt.c;
     for (uint32_t li = 0; li < n; li++) {
@@ -557,7 +731,7 @@ __device__ __forceinline__ C4 shade_spot(const LyapPoint &pt, V3 camC, const Lya
 __device__ __forceinline__ C4 shade_directional(const LyapPoint &pt, const LyapLight *lights, uint32_t n)
 {
     C4 color{0.f, 0.f, 0.f, 0.f};
-    if (isnan(pt.a)) return color;
+    if (f_isnan(pt.a)) return color;
     const V3 N = v3(pt.N);
     for (uint32_t li = 0; li < n; li++) {
         const LyapLight &L = lights[li];

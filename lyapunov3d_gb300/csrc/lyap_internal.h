@@ -6,34 +6,9 @@
 #include <stdint.h>
 
 #include "lyap_gb300.h"
+#include "lyap_jobs.h"
 
 namespace lyapgb {
-
-// One frame to render: everything kernel_calc_render receives (kernel.cu:500)
-// plus the image size, the lambda form and optional outputs.
-struct RenderJob {
-    LyapCam cam;                 // already recalculated (scene_cam_recalculate)
-    LyapParams prm;
-    const int32_t *seq;          // device, -1 terminated
-    const LyapLight *lights;     // device, n_lights entries (recalculated)
-    RGBA *rgba;                  // device, width*height
-    LyapPoint *points;           // device, width*height
-    uint32_t *counts;            // device, 3 per pixel, or null
-    uint32_t seq_period;         // entries before the terminator
-    uint32_t n_lights;
-    uint32_t width, height;
-    uint32_t light_model;        // LYAP_LIGHT_SPOT | LYAP_LIGHT_DIRECTIONAL
-    uint32_t pad_;
-};
-
-struct VolumeJob {
-    float *out;                  // device, nx*ny*nz, x fastest
-    const int32_t *seq;
-    LyapParams prm;
-    uint32_t seq_period;
-    uint32_t nx, ny, nz;
-    float lo[3], hi[3];
-};
 
 // kernels launchers (lyap_render.cu, lyap_volume.cu); return a cudaError_t
 cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_counter,

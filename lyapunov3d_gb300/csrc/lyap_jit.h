@@ -1,0 +1,34 @@
+// lyap_jit.h -- run-time specialisation of the kernels (lyap_jit.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "lyap_jobs.h"
+
+// Launch shape of the specialised kernels: with the sequence compiled in,
+// the render kernel fits in 80 registers without spilling (6 blocks of 128
+// threads per SM, against 4 for the precompiled kernel) and the volume sweep
+// evaluates LYAP_JIT_VOLUME_K voxels per thread in 64 registers (4 blocks of
+// 256 threads per SM).
+#define LYAP_JIT_MAX_PERIOD 32
+#define LYAP_JIT_RENDER_MIN_BLOCKS 6
+#define LYAP_RENDER_THREADS_JIT 128
+#define LYAP_JIT_VOLUME_K 2
+#define LYAP_JIT_VOLUME_MIN_BLOCKS 4
+#define LYAP_VOLUME_THREADS_JIT 256
+
+namespace lyapgb {
+
+// Both return 1 when the specialised kernel was launched (its launch status
+// in *launch_err) and 0 when the path is unavailable for this call (reason
+// in *why); the caller then launches the precompiled kernel.
+int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq, uint32_t *d_work_counter,
+                      unsigned long long *d_stats, uint32_t blocks_per_sm, uint32_t threads, cudaStream_t stream,
+                      cudaError_t *launch_err, std::string *why);
+int jit_launch_volume(const VolumeJob &job, uint32_t mode, const int32_t *h_seq, unsigned long long *d_stats,
+                      uint32_t blocks_per_sm, uint32_t threads, cudaStream_t stream, cudaError_t *launch_err,
+                      std::string *why);
+
+}  // namespace lyapgb

@@ -1,0 +1,410 @@
+// lyap_kernels.cuh -- the raymarch and volume kernels as templates over the
+// lambda evaluator.  Compiled twice: into the library by nvcc with
+// RuntimeLambda (any sequence, read from device memory), and at run time by
+// NVRTC with ConstLambda (the caller's sequence baked in as template
+// constants, lyap_jit.cpp).
+//
+// render_persistent (kernel_calc_render, kernel.cu:500).  Every lambda
+// sample of a ray costs the same (settle + accum map iterations), but rays
+// need 0 to ~depth*nearMultiplier samples.  A thread-per-pixel kernel (the
+// reference's) keeps a warp busy until its longest ray ends.  Here each
+// lane of a persistent warp owns one ray at a time; after every sample the
+// lanes whose ray ended write their pixel and take the next pixel from a
+// global queue, so all 32 lanes evaluate a sample in every round until the
+// queue is empty.  The lambda loop is uniform across the warp.
+//
+// volume_sweep (kernel_calc_volume, kernel.cu:518).  Every voxel costs the
+// same; each warp takes 32*K consecutive voxels, K per lane, evaluated as K
+// interleaved dependency chains, and stores them with coalesced streaming
+// 128-byte stores (st.global.cs: written once, never read back here).
+#pragma once
+
+#include "lyap_device.cuh"
+#include "lyap_jobs.h"
+
+#ifndef LYAP_RENDER_THREADS
+#define LYAP_RENDER_THREADS 128
+#endif
+#ifndef LYAP_RENDER_MIN_BLOCKS
+#define LYAP_RENDER_MIN_BLOCKS 4
+#endif
+#ifndef LYAP_VOLUME_THREADS
+#define LYAP_VOLUME_THREADS 256
+#endif
+#ifndef LYAP_VOLUME_MIN_BLOCKS
+#define LYAP_VOLUME_MIN_BLOCKS 2
+#endif
+
+namespace lyapgb {
+
+constexpr uint32_t FULL = 0xffffffffu;
+
+// ------------------------------------------------------ lambda evaluators
+// Any sequence: period and symbols read from device memory per warp.
+template <uint32_t MODE>
+struct RuntimeLambda {
+    SeqInfo si;
+    __device__ __forceinline__ RuntimeLambda(const int32_t *seq, uint32_t period, const LyapParams &prm)
+        : si(seq_setup(seq, period, prm)) {}
+    __device__ __forceinline__ float operator()(float x, float y, float z, bool &skipped, bool &fallback) const
+    {
+        return eval_lambda<MODE>(x, y, z, si, skipped, fallback);
+    }
+    template <int K>
+    __device__ __forceinline__ void eval(const float (&x)[K], const float (&y)[K], const float (&z)[K],
+                                         float (&out)[K], uint32_t &skipped, uint32_t &fallback) const
+    {
+        skipped = fallback = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            bool sk, fb;
+            out[k] = eval_lambda<MODE>(x[k], y[k], z[k], si, sk, fb);
+            skipped |= (sk ? 1u : 0u) << k;
+            fallback |= (fb ? 1u : 0u) << k;
+        }
+    }
+};
+
+// The sequence fixed at compile time: SS = symbols of period positions
+// 0..L-1, SA = the same rotated to where accumulation starts (OA = settle
+// mod L).  The constructor checks the device sequence and the settle count
+// against the constants; on any mismatch it evaluates with the runtime path
+// instead, so a stale specialisation can cost speed but never correctness.
+template <uint32_t MODE, uint32_t OA, class SS, class SA>
+struct ConstLambda {
+    SeqInfo si;
+    bool match;
+    __device__ __forceinline__ ConstLambda(const int32_t *seq, uint32_t period, const LyapParams &prm)
+    {
+        si.seq = seq;
+        si.L = period;
+        si.S = prm.settle;
+        si.A = prm.accum;
+        si.d = prm.d;
+        si.oA = prm.settle % (period ? period : 1u);
+        si.wS = si.wA = 0;
+        bool ok = (period == (uint32_t)SS::L) && (prm.settle % (uint32_t)SS::L == OA);
+        if (ok) {
+            for (uint32_t j = 0; j < period; j++) ok = ok && ((uint32_t)seq[j] == SS::at_rt(j));
+        }
+        match = ok;
+    }
+    __device__ __forceinline__ float operator()(float x, float y, float z, bool &skipped, bool &fallback) const
+    {
+        if (match) {
+            const float px[1] = {x}, py[1] = {y}, pz[1] = {z};
+            float o[1];
+            uint32_t sk, fb;
+            lambda_const<MODE, 1, SS, SA>(px, py, pz, si.d, si.S, si.A, o, sk, fb);
+            skipped = sk != 0;
+            fallback = fb != 0;
+            return o[0];
+        }
+        return lambda_generic<MODE>(x, y, z, si, skipped, fallback);
+    }
+    template <int K>
+    __device__ __forceinline__ void eval(const float (&x)[K], const float (&y)[K], const float (&z)[K],
+                                         float (&out)[K], uint32_t &skipped, uint32_t &fallback) const
+    {
+        if (match) {
+            lambda_const<MODE, K, SS, SA>(x, y, z, si.d, si.S, si.A, out, skipped, fallback);
+            return;
+        }
+        skipped = fallback = 0;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            bool sk, fb;
+            out[k] = lambda_generic<MODE>(x[k], y[k], z[k], si, sk, fb);
+            skipped |= (sk ? 1u : 0u) << k;
+            fallback |= (fb ? 1u : 0u) << k;
+        }
+    }
+};
+
+// -------------------------------------------------------------- outputs
+struct LaneStats {
+    uint32_t samples, skipped, march, hone, normal, hits, rays, fallback, spec, spec_used;
+    uint32_t rounds, lane_rounds;   // per warp, kept by every lane alike
+};
+
+// position of the n-th (0-based) set bit of mask; mask has more than n bits set
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t mask, uint32_t n)
+{
+    for (uint32_t i = 0; i < n; i++) mask &= mask - 1u;
+    return (uint32_t)(__ffs(mask) - 1);
+}
+
+__device__ __forceinline__ void store_point(LyapPoint *dst, const Ray &r, bool hit)
+{
+    float *f = reinterpret_cast<float *>(dst);
+    if (hit) {
+        f[0] = r.P.x; f[1] = r.P.y; f[2] = r.P.z;
+        f[3] = r.N.x; f[4] = r.N.y; f[5] = r.N.z;
+        f[6] = r.a; f[7] = r.c; f[8] = r.l;
+    } else {
+        // a miss: all-NaN bytes (the reference leaves the point unwritten)
+        const float nanf_ = __int_as_float(-1);
+#pragma unroll
+        for (int k = 0; k < 9; k++) f[k] = nanf_;
+    }
+}
+
+// Write one finished pixel: point, colour, optional per-pixel sample counts.
+__device__ __forceinline__ void finish_pixel(RGBA *rgba, LyapPoint *points, uint32_t *counts, uint32_t ind,
+                                             const Ray &r, bool hit, V3 camC, const LyapLight *lights,
+                                             uint32_t n_lights, uint32_t light_model, LaneStats &st)
+{
+    store_point(points + ind, r, hit);
+    uint32_t px = 0;
+    if (hit) {
+        LyapPoint pt;
+        pt.P = LyapVec{r.P.x, r.P.y, r.P.z};
+        pt.N = LyapVec{r.N.x, r.N.y, r.N.z};
+        pt.a = r.a;
+        pt.c = r.c;
+        pt.l = r.l;
+        C4 col = (light_model == LYAP_LIGHT_DIRECTIONAL) ? shade_directional(pt, lights, n_lights)
+                                                         : shade_spot(pt, camC, lights, n_lights);
+        px = (uint32_t)to_byte(col.x) | ((uint32_t)to_byte(col.y) << 8) | ((uint32_t)to_byte(col.z) << 16) |
+             ((uint32_t)to_byte(col.w) << 24);
+    }
+    reinterpret_cast<uint32_t *>(rgba)[ind] = px;
+    if (counts) {
+        counts[3 * (size_t)ind + 0] = r.nm;
+        counts[3 * (size_t)ind + 1] = r.nh;
+        counts[3 * (size_t)ind + 2] = hit ? 6u : 0u;
+    }
+    st.march += r.nm;
+    st.hone += r.nh;
+    st.normal += hit ? 6u : 0u;
+    st.hits += hit ? 1u : 0u;
+    st.rays += 1;
+}
+
+__device__ __forceinline__ void flush_stats(unsigned long long *stats, const LaneStats &st, uint32_t mask)
+{
+    if (!stats) return;
+    const uint32_t v[10] = {st.samples, st.skipped, st.march, st.hone, st.normal,
+                            st.hits, st.rays, st.fallback, st.spec, st.spec_used};
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(mask) - 1;
+#pragma unroll
+    for (int k = 0; k < 10; k++) {
+        const uint32_t s = __reduce_add_sync(mask, v[k]);
+        if (lane == leader && s) atomicAdd(stats + k, (unsigned long long)s);
+    }
+    if (lane == leader && st.rounds) {
+        atomicAdd(stats + LYAP_STAT_ROUNDS, (unsigned long long)st.rounds);
+        atomicAdd(stats + LYAP_STAT_LANE_ROUNDS, (unsigned long long)st.lane_rounds);
+        atomicMax(stats + LYAP_STAT_MAX_ROUNDS, (unsigned long long)st.rounds);
+    }
+}
+
+// ----------------------------------------------------------------- render
+template <class Lam>
+__global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
+    render_persistent(const __grid_constant__ RenderJob job, uint32_t *__restrict__ work_counter,
+                      unsigned long long *__restrict__ stats)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t npix = job.width * job.height;
+    const Lam lam(job.seq, job.seq_period, job.prm);
+    const CamRays cr = cam_rays(job.cam);
+    // march positions are known ahead only with a fixed step length
+    const bool spec_ok = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f) &&
+                         !(job.flags & LYAP_FLAG_NO_SPECULATION);
+    LaneStats st = {};
+    Ray r;
+    r.phase = PH_MARCH0;
+    uint32_t pix = 0;
+    bool active = false, drained = false;
+
+    for (;;) {
+        // refill the lanes whose ray has ended
+        for (;;) {
+            const bool need = !active && !drained;
+            const uint32_t mask = __ballot_sync(FULL, need);
+            if (mask == 0) break;
+            const uint32_t leader = __ffs(mask) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(work_counter, (uint32_t)__popc(mask));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const uint32_t my = base + __popc(mask & ((1u << lane) - 1u));
+                if (my >= npix) {
+                    drained = true;
+                } else {
+                    pix = my;
+                    const uint32_t sx = my % job.width, sy = my / job.width;
+                    if (ray_init(r, cr, job.prm, sx, sy)) {
+                        active = true;
+                    } else {
+                        r.nm = r.nh = 0;
+                        finish_pixel(job.rgba, job.points, job.counts, my, r, false, cr.C, job.lights,
+                                     job.n_lights, job.light_model, st);
+                    }
+                }
+            }
+        }
+        const uint32_t amask = __ballot_sync(FULL, active);
+        if (amask == 0) break;
+
+        // Speculation in the tail.  Once the queue is empty, lanes without a
+        // ray evaluate, for the rays still running in this warp, the samples
+        // those rays will ask for next.  That is only possible where the next
+        // positions do not depend on the lambdas still to come: march steps
+        // when the step length is fixed (no jitter, near multiplier 1), and
+        // the six normal samples.  Helper lane (owner, j) takes the owner's
+        // j-th sample ahead; the owner feeds the results to its state machine
+        // in order and drops the rest once the ray leaves that phase.
+        uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
+        bool helper = false;
+        uint32_t owner = lane, offset = 0;
+        if (spec_ok && amask != FULL) {
+            const bool elig = active && (r.phase <= PH_MARCH || (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5));
+            emask = __ballot_sync(FULL, elig);
+            ne = __popc(emask);
+            if (ne) {
+                imask = ~amask;
+                ni = __popc(imask);
+                maxj = (ni + ne - 1) / ne;
+                if (!active) {
+                    const uint32_t rank = __popc(imask & ((1u << lane) - 1u));
+                    owner = nth_set_bit(emask, rank % ne);
+                    offset = 1 + rank / ne;
+                    helper = true;
+                }
+            }
+        }
+        V3 Q = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
+        if (ne) {
+            // every lane reads its owner's state (its own, for non-helpers)
+            V3 oP, oV;
+            oP.x = __shfl_sync(FULL, r.P.x, owner);
+            oP.y = __shfl_sync(FULL, r.P.y, owner);
+            oP.z = __shfl_sync(FULL, r.P.z, owner);
+            oV.x = __shfl_sync(FULL, r.V.x, owner);
+            oV.y = __shfl_sync(FULL, r.V.y, owner);
+            oV.z = __shfl_sync(FULL, r.V.z, owner);
+            const float odt = __shfl_sync(FULL, r.dt, owner);
+            const float omag = __shfl_sync(FULL, r.mag, owner);
+            const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
+            if (helper) {
+                if (ophase <= PH_MARCH) {
+                    // the position after `offset` more fixed steps, added one by one as ray_advance does
+                    for (uint32_t j = 0; j < offset; j++) oP = oP + oV * odt;
+                    Q = oP;
+                } else {
+                    Ray tmp;
+                    tmp.P = oP;
+                    tmp.mag = omag;
+                    const uint32_t k = ophase - PH_NORM0 + offset;
+                    tmp.phase = PH_NORM0 + (k > 5 ? 5 : k);
+                    Q = ray_sample_point(tmp);
+                }
+                st.spec += 1;
+            }
+        }
+
+        // one lambda sample for every lane (idle lanes evaluate a dummy point)
+        st.rounds += 1;
+        st.lane_rounds += __popc(amask) + (ne ? (ni < maxj * ne ? ni : maxj * ne) : 0u);
+        bool skipped, fallback;
+        const float lam_v = lam(Q.x, Q.y, Q.z, skipped, fallback);
+        int res = RAY_CONTINUE;
+        uint32_t kind = 0;   // 1: march, 2: normal
+        if (active) {
+            kind = (r.phase <= PH_MARCH) ? 1u : (r.phase >= PH_NORM0 ? 2u : 0u);
+            st.samples += 1;
+            st.skipped += skipped ? 1u : 0u;
+            st.fallback += fallback ? 1u : 0u;
+            res = ray_advance(r, lam_v, job.prm);
+        }
+        if (ne) {
+            const bool own_elig = (emask >> lane) & 1u;
+            const uint32_t idx = __popc(emask & ((1u << lane) - 1u));
+            const uint32_t sk_bits = (skipped ? 1u : 0u) | (fallback ? 2u : 0u);
+            for (uint32_t j = 1; j <= maxj; j++) {
+                const uint32_t rr = (j - 1) * ne + idx;
+                const bool have = own_elig && rr < ni;
+                const uint32_t src = have ? nth_set_bit(imask, rr) : lane;
+                const float lj = __shfl_sync(FULL, lam_v, src);
+                const uint32_t bj = __shfl_sync(FULL, sk_bits, src);
+                const bool same_phase = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
+                if (have && res == RAY_CONTINUE && same_phase) {
+                    st.samples += 1;
+                    st.skipped += bj & 1u;
+                    st.fallback += (bj >> 1) & 1u;
+                    st.spec_used += 1;
+                    res = ray_advance(r, lj, job.prm);
+                }
+            }
+        }
+        if (active && res != RAY_CONTINUE) {
+            finish_pixel(job.rgba, job.points, job.counts, pix, r, res == RAY_HIT, cr.C, job.lights, job.n_lights,
+                         job.light_model, st);
+            active = false;
+        }
+    }
+    flush_stats(stats, st, FULL);
+}
+
+// ----------------------------------------------------------------- volume
+__device__ __forceinline__ float voxel_coord(float lo, float hi, uint32_t i, uint32_t n)
+{
+    return lo + ((hi - lo) * (float)i) / (float)n;
+}
+
+template <class Lam, int K>
+__global__ void __launch_bounds__(LYAP_VOLUME_THREADS, LYAP_VOLUME_MIN_BLOCKS)
+    volume_sweep(const __grid_constant__ VolumeJob job, unsigned long long *__restrict__ stats)
+{
+    const Lam lam(job.seq, job.seq_period, job.prm);
+    const uint64_t nxy = (uint64_t)job.nx * job.ny;
+    const uint64_t total = nxy * job.nz;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint64_t nwork = (total + 32u * K - 1) / (32u * K);
+    const uint64_t wstride = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    uint32_t skipped_n = 0, fallback_n = 0, samples = 0;
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwork; w += wstride) {
+        float px[K], py[K], pz[K], out[K];
+        uint64_t idx[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            uint64_t i = w * (32u * K) + 32u * k + lane;
+            idx[k] = i;
+            if (i >= total) i = total - 1;
+            const uint32_t z = (uint32_t)(i / nxy);
+            const uint64_t rxy = i - (uint64_t)z * nxy;
+            const uint32_t y = (uint32_t)(rxy / job.nx);
+            const uint32_t x = (uint32_t)(rxy - (uint64_t)y * job.nx);
+            px[k] = voxel_coord(job.lo[0], job.hi[0], x, job.nx);
+            py[k] = voxel_coord(job.lo[1], job.hi[1], y, job.ny);
+            pz[k] = voxel_coord(job.lo[2], job.hi[2], z, job.nz);
+        }
+        uint32_t sk, fb;
+        lam.template eval<K>(px, py, pz, out, sk, fb);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if (idx[k] < total) {
+                __stcs(job.out + idx[k], out[k]);
+                samples += 1;
+                skipped_n += (sk >> k) & 1u;
+                fallback_n += (fb >> k) & 1u;
+            }
+        }
+    }
+    if (stats) {
+        const uint32_t mask = __activemask();
+        const uint32_t s0 = __reduce_add_sync(mask, samples);
+        const uint32_t s1 = __reduce_add_sync(mask, skipped_n);
+        const uint32_t s7 = __reduce_add_sync(mask, fallback_n);
+        if (lane == (uint32_t)(__ffs(mask) - 1)) {
+            if (s0) atomicAdd(stats + ST_SAMPLES, (unsigned long long)s0);
+            if (s1) atomicAdd(stats + ST_SKIPPED, (unsigned long long)s1);
+            if (s7) atomicAdd(stats + ST_FALLBACK, (unsigned long long)s7);
+        }
+    }
+}
+
+}  // namespace lyapgb

@@ -34,14 +34,22 @@ class DeviceFrame:
         self.d_counts = torch.zeros(n * 3, dtype=torch.int32, device=device) if counts else None
         self.d_stats = torch.zeros(capi.STAT_COUNT, dtype=torch.int64, device=device) if stats else None
 
-    def ext(self, variant=capi.VARIANT_PLAIN, **kw):
+    def ext(self, variant=capi.VARIANT_PLAIN, jit=False, **kw):
+        """jit: hand the host copy of the sequence over so the library uses the
+        kernels compiled for it at run time (identical results, faster; the
+        first call per sequence pays a few seconds of compilation); False
+        forces the precompiled kernels."""
+        if jit:
+            kw.setdefault("h_seq", self.seq.ctypes.data)
+        else:
+            kw["flags"] = kw.get("flags", 0) | capi.FLAG_NO_JIT
         return capi.LyapRenderExt(variant=variant, light_model=self.light_model,
                                   d_counts=self.d_counts.data_ptr() if self.d_counts is not None else None,
                                   d_stats=self.d_stats.data_ptr() if self.d_stats is not None else None, **kw)
 
-    def run(self, variant=capi.VARIANT_PLAIN, stream=None, **kw):
+    def run(self, variant=capi.VARIANT_PLAIN, stream=None, jit=False, **kw):
         capi.render(self.cam, self.prm, self.d_seq, self.seq.size, self.d_lights, len(self.lights), self.d_rgba,
-                    self.d_points, self.width, self.height, ext=self.ext(variant, **kw), stream=stream)
+                    self.d_points, self.width, self.height, ext=self.ext(variant, jit, **kw), stream=stream)
 
     def reset_stats(self):
         if self.d_stats is not None:
@@ -78,13 +86,17 @@ class DeviceVolume:
         self.d_out = torch.empty(self.nx * self.ny * self.nz, dtype=torch.float32, device=device)
         self.d_stats = torch.zeros(capi.STAT_COUNT, dtype=torch.int64, device=device) if stats else None
 
-    def ext(self, variant=capi.VARIANT_PLAIN, **kw):
+    def ext(self, variant=capi.VARIANT_PLAIN, jit=False, **kw):
+        if jit:
+            kw.setdefault("h_seq", self.seq.ctypes.data)
+        else:
+            kw["flags"] = kw.get("flags", 0) | capi.FLAG_NO_JIT
         return capi.LyapVolumeExt(variant=variant,
                                   d_stats=self.d_stats.data_ptr() if self.d_stats is not None else None, **kw)
 
-    def run(self, variant=capi.VARIANT_PLAIN, stream=None, **kw):
+    def run(self, variant=capi.VARIANT_PLAIN, stream=None, jit=False, **kw):
         capi.volume(self.d_out, self.nx, self.ny, self.nz, self.wl.lo, self.wl.hi, self.prm, self.d_seq,
-                    self.seq.size, ext=self.ext(variant, **kw), stream=stream)
+                    self.seq.size, ext=self.ext(variant, jit, **kw), stream=stream)
 
     def reset_stats(self):
         if self.d_stats is not None:
