@@ -55,6 +55,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--volume", type=int, default=512, help="edge of the secondary volume sweep (0 = skip)")
     ap.add_argument("--no-jit", action="store_true", help="precompiled kernels only (no run-time specialisation)")
+    ap.add_argument("--report", choices=["precision"], default=None,
+                    help="instead of the benchmark, print the precision form's error report")
     return ap.parse_args()
 
 
@@ -412,8 +414,82 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_precision_report(args):
+    """The precision form on the CPU-runnable workload (ABC, 20 + 100, [2.5, 4]^3):
+    lambda of the plain, product and FP64 forms at 2^20 seeded points against
+    the FP64 oracle; a 128^2 frame rendered with the product form and FP64
+    bisection (20 halvings) of every crossing, its hit-point lambdas against
+    the oracle, and its surface agreement with the plain frame."""
+    import torch
+    from lyapunov3d_gb300 import capi, scenes
+    from lyapunov3d_gb300.device import DeviceFrame
+    from oracle import ORC_F64, Oracle
+    dev = torch.device("cuda", 0)
+    orc = Oracle()
+    wl = scenes.small_render(128)
+    prm = wl.params
+    seq = capi.seq_parse(wl.seq)
+    d_seq = torch.from_numpy(seq).to(dev)
+    n = 1 << 20
+    pts = np.random.default_rng(20240).uniform(prm.lMin, prm.lMax, size=(n, 3)).astype(np.float32)
+    d_xyz = torch.from_numpy(pts.reshape(-1)).to(dev)
+    pts4 = np.column_stack([pts.astype(np.float64), np.full(n, prm.d)])
+    t0 = time.perf_counter()
+    ref = orc.lyap4d(ORC_F64, pts4, prm.settle, prm.accum, seq)
+    t_orc = time.perf_counter() - t0
+    fin = np.isfinite(ref)
+
+    def stats(got):
+        g = got.astype(np.float64)
+        ok = fin & np.isfinite(g)
+        d = np.abs(g[ok] - ref[ok])
+        return {"max_abs": float(d.max()), "mean_abs": float(d.mean()), "median_abs": float(np.median(d)),
+                "p99_abs": float(np.quantile(d, 0.99)), "nan_mismatch": int((np.isnan(g) != np.isnan(ref)).sum())}
+    out = {}
+    o32 = torch.empty(n, dtype=torch.float32, device=dev)
+    o64 = torch.empty(n, dtype=torch.float64, device=dev)
+    for name, form in [("plain", capi.VARIANT_PLAIN), ("product", capi.VARIANT_PRODUCT)]:
+        capi.lambda_points(d_xyz, n, prm, d_seq, seq.size, form, o32)
+        out[name] = stats(o32.cpu().numpy())
+    capi.lambda_points(d_xyz, n, prm, d_seq, seq.size, capi.FORM_F64, o64)
+    out["f64_gpu"] = stats(o64.cpu().numpy())
+
+    f = DeviceFrame(wl, device=dev, counts=True)
+    f.run(capi.VARIANT_PLAIN)
+    plain_pts = f.points().copy()
+    f.reset_stats()
+    f.run(capi.VARIANT_PRODUCT, flags=capi.FLAG_BISECT_F64, bisect_halvings=20)
+    torch.cuda.synchronize()
+    pp = f.points()
+    hit, phit = ~np.isnan(pp["a"]), ~np.isnan(plain_pts["a"])
+    P = pp["P"][hit].astype(np.float32)
+    href = orc.lyap4d(ORC_F64, np.column_stack([P.astype(np.float64), np.full(len(P), prm.d)]), prm.settle,
+                      prm.accum, seq)
+    d_P = torch.from_numpy(np.ascontiguousarray(P).reshape(-1)).to(dev)
+    hp = torch.empty(len(P), dtype=torch.float32, device=dev)
+    capi.lambda_points(d_P, len(P), prm, d_seq, seq.size, capi.VARIANT_PRODUCT, hp)
+    hp = hp.cpu().numpy().astype(np.float64)
+    ok = np.isfinite(href) & np.isfinite(hp)
+    stored = pp["l"][hit].astype(np.float64)
+    ok2 = np.isfinite(href) & np.isfinite(stored)
+    report = {
+        "workload": wl.name, "points": n, "oracle_seconds": t_orc, "oracle_threads": orc.threads(),
+        "lambda_vs_f64_oracle_at_points": out,
+        "frame": {"pixels": int(hit.size), "hits": int(hit.sum()), "plain_hits": int(phit.sum()),
+                  "surface_pixel_agreement_vs_plain": float((hit == phit).mean()),
+                  "hit_lambda_product_vs_f64": {"max_abs": float(np.abs(hp[ok] - href[ok]).max()),
+                                                "mean_abs": float(np.abs(hp[ok] - href[ok]).mean())},
+                  "hit_lambda_stored_vs_f64": {"max_abs": float(np.abs(stored[ok2] - href[ok2]).max())},
+                  "halvings": 20},
+    }
+    print(json.dumps(report), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.report == "precision":
+        run_precision_report(args)
+        return
     if args.impl == "reference":
         run_reference_arm(args)
     else:

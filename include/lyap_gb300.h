@@ -225,6 +225,13 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_FLAG_REQUIRE_JIT 2u  /* fail (LYAP_ERR_JIT) instead of falling back */
 #define LYAP_FLAG_NO_SPECULATION 4u /* render: idle lanes do not take samples
                                        ahead for running rays (same results) */
+#define LYAP_FLAG_BISECT_F64  8u  /* render, precision form: instead of the
+                                     reference's honing, bisect each ray's
+                                     crossing [last sample above, first at or
+                                     below the opaque threshold] bisect_halvings
+                                     times (default 20) with lambda in double;
+                                     the point's l is then the double lambda at
+                                     the stored (float) point */
 
 typedef struct {
     uint32_t size;               /* = sizeof(LyapRenderExt) */
@@ -237,6 +244,8 @@ typedef struct {
     uint32_t blocks_per_sm;      /* launch shape, 0 = automatic */
     uint32_t threads_per_block;  /* multiple of 32, <= 128; 0 = automatic */
     const int32_t *h_seq;        /* optional host copy of d_seq (seq_len entries) */
+    uint32_t bisect_halvings;    /* LYAP_FLAG_BISECT_F64: halvings (0 = 20) */
+    uint32_t pad_;
 } LyapRenderExt;
 
 typedef struct {
@@ -313,6 +322,16 @@ int lyap_kernel_calc_render(uint32_t grid_x, uint32_t grid_y, uint32_t block_x, 
                             int32_t *d_seq, LyapLight *d_lights, uint32_t n_lights, void *stream);
 int lyap_kernel_calc_volume(const uint32_t grid[3], const uint32_t block[3], float *d_exps,
                             const LyapParams *prm, int32_t *d_seq, void *stream);
+
+/* lyap4d (kernel.cu:108-154) at n arbitrary points: d_xyz holds x, y, z per
+ * point (device, 3*n floats), symbol D takes prm->d; d_out receives n
+ * lambdas in the form `form` (LYAP_VARIANT_PLAIN, LYAP_VARIANT_PRODUCT, or
+ * LYAP_FORM_F64: the double-precision evaluator of the precision form's
+ * bisection, whose orbit is the reference's DOUBLE_REALS arithmetic).
+ * d_out is float[n], or double[n] for LYAP_FORM_F64. */
+#define LYAP_FORM_F64 2u
+int lyap_lambda_points(const float *d_xyz, size_t n, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
+                       uint32_t form, void *d_out, void *stream);
 
 /* lyap_render without any device allocation.  It has no counterpart in the
  * reference (whose front-ends cudaMalloc everything up front).  For callers

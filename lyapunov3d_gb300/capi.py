@@ -29,6 +29,8 @@ LYAP_ERR_JIT = -7
 FLAG_NO_JIT = 1
 FLAG_REQUIRE_JIT = 2
 FLAG_NO_SPECULATION = 4
+FLAG_BISECT_F64 = 8
+FORM_F64 = 2
 
 VARIANT_PLAIN = 0
 VARIANT_PRODUCT = 1
@@ -52,7 +54,8 @@ class LyapError(RuntimeError):
 class LyapRenderExt(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("variant", c_uint32), ("light_model", c_uint32), ("flags", c_uint32),
                 ("d_counts", c_void_p), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
-                ("threads_per_block", c_uint32), ("h_seq", c_void_p)]
+                ("threads_per_block", c_uint32), ("h_seq", c_void_p), ("bisect_halvings", c_uint32),
+                ("pad_", c_uint32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -76,7 +79,8 @@ class LyapVolumeExt(ctypes.Structure):
 EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string",
             "lyap_seq_parse", "lyap_cam_recalculate", "lyap_lights_recalculate", "lyap_render",
             "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
-            "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc", "lyap_jit_info"]
+            "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc", "lyap_jit_info",
+            "lyap_lambda_points"]
 
 
 def _load():
@@ -105,6 +109,7 @@ def _load():
                                           c_void_p]
     L.lyap_pipe_probe.argtypes = [c_uint32, c_uint32, c_void_p, POINTER(ctypes.c_double), c_void_p]
     L.lyap_jit_info.argtypes = [ctypes.c_char_p, c_size_t]
+    L.lyap_lambda_points.argtypes = [c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p]
     for name in EXPORTED:
         if name not in ("lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string"):
             getattr(L, name).restype = c_int
@@ -216,6 +221,12 @@ def kernel_calc_volume(grid, block, d_exps, prm, d_seq, stream=None):
     g = (c_uint32 * 3)(*grid)
     b = (c_uint32 * 3)(*block)
     _check(lib.lyap_kernel_calc_volume(g, b, _vp(d_exps), ctypes.byref(prm), _vp(d_seq), _stream(stream)))
+
+
+def lambda_points(d_xyz, n, prm, d_seq, seq_len, form, d_out, stream=None):
+    """lyap_lambda_points: lambda at n points (x, y, z per point) in the given form."""
+    _check(lib.lyap_lambda_points(_vp(d_xyz), n, ctypes.byref(prm), _vp(d_seq), seq_len, form, _vp(d_out),
+                                  _stream(stream)))
 
 
 def pipe_probe(kind, iters, d_sink, stream=None):

@@ -170,10 +170,22 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     RenderJob job = make_job(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext);
     // scratch: the pixel queue's counter, stream-ordered so concurrent calls
     // on different streams each get their own
+    // precision form with FP64 bisection: also the per-pixel crossing
+    // brackets and the list of pixels that crossed (scratch of the two passes)
+    const bool bisect = ext && (ext->flags & LYAP_FLAG_BISECT_F64);
+    const size_t npix = (size_t)width * height;
+    const size_t scratch = bisect ? 256 + (npix + 1) * sizeof(uint32_t) + 256 + npix * 2 * sizeof(float)
+                                  : sizeof(uint32_t);
     uint32_t *d_counter = nullptr;
-    cudaError_t e = cudaMallocAsync((void **)&d_counter, sizeof(uint32_t), s);
+    cudaError_t e = cudaMallocAsync((void **)&d_counter, scratch, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: scratch allocation");
     e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s);
+    if (e == cudaSuccess && bisect) {
+        char *base = reinterpret_cast<char *>(d_counter);
+        job.hits = reinterpret_cast<uint32_t *>(base + 256);
+        job.bracket = reinterpret_cast<float *>(base + 256 + (((npix + 1) * sizeof(uint32_t) + 255) & ~(size_t)255));
+        e = cudaMemsetAsync(job.hits, 0, sizeof(uint32_t), s);
+    }
     if (e == cudaSuccess) {
         const uint32_t variant = ext ? ext->variant : LYAP_VARIANT_PLAIN;
         const uint32_t flags = ext ? ext->flags : 0u;
@@ -196,6 +208,8 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
         if (!launched)
             e = launch_render(job, variant, d_counter, ext ? ext->d_stats : nullptr, ext ? ext->blocks_per_sm : 0,
                               ext ? ext->threads_per_block : 0, s);
+        if (e == cudaSuccess && bisect)
+            e = launch_bisect(job, variant, ext->bisect_halvings ? ext->bisect_halvings : 20u, ext->d_stats, s);
     }
     cudaError_t e2 = cudaFreeAsync(d_counter, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: launch");

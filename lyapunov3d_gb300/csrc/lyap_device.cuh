@@ -482,6 +482,77 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
     }
 }
 
+// ------------------------------------------------------- lambda in double
+// The FP64 evaluator used by the precision form's bisection and by
+// lyap_lambda_points: the reference's DOUBLE_REALS arithmetic for the orbit
+// (v = r*v*(1-v) and d = r - 2r*v, each product and difference rounded once
+// in double, kernel.cu:135,143-144 with Real = double), so the orbit is
+// bit-identical to the FP64 oracle's; the logarithms are accumulated as a
+// running double product renormalised by exponent extraction every 16 steps
+// with one log2 per sample (a block ending outside [2^-900, 2^900], or a
+// zero factor, redoes the sample with one log per step).  Agrees with the
+// per-step-log oracle to ~1e-13 relative.
+__device__ __forceinline__ double pick_d(uint32_t sym, double x, double y, double z, double d)
+{
+    double lo = (sym & 1u) ? y : x;
+    double hi = (sym & 1u) ? d : z;
+    return (sym & 2u) ? hi : lo;
+}
+
+static __device__ __noinline__ double lambda_f64(double x, double y, double z, const SeqInfo &si)
+{
+    const double d = (double)si.d;
+    const int32_t *seq = si.seq;
+    const uint32_t L = si.L;
+    double v = 0.5;
+    uint32_t k = 0;
+    for (uint32_t n = 0; n < si.S; n++) {
+        const double r = pick_d((uint32_t)seq[k] & 3u, x, y, z, d);
+        k = (k + 1 == L) ? 0 : k + 1;
+        v = r * v * (1.0 - v);
+    }
+    if (!((v - 0.5 <= -1e-8) || (v - 0.5 >= 1e-8))) return 0.0 / (double)si.A;
+    const uint32_t kA = k;
+    const double vA = v;
+    double p = 1.0;
+    int64_t e = 0;
+    bool bad = false;
+    for (uint32_t n = 0; n < si.A; n++) {
+        const double r = pick_d((uint32_t)seq[k] & 3u, x, y, z, d);
+        k = (k + 1 == L) ? 0 : k + 1;
+        v = r * v * (1.0 - v);
+        double dd = r - 2.0 * r * v;
+        p = p * fabs(dd);
+        if ((n & 15u) == 15u || n + 1 == si.A) {
+            const uint64_t bits = (uint64_t)__double_as_longlong(p);
+            const int64_t ef = (int64_t)((bits >> 52) & 0x7ffu);
+            if (ef < 123 || ef > 1923) bad = true;   // outside [2^-900, 2^900], zero, inf or NaN
+            e += ef - 1023;
+            p = __longlong_as_double((long long)((bits & 0x000fffffffffffffull) | 0x3ff0000000000000ull));
+        }
+    }
+    double l;
+    if (bad) {
+        // one log per step, as the oracle does, from the start of accumulation
+        v = vA;
+        k = kA;
+        l = 0.0;
+        for (uint32_t n = 0; n < si.A; n++) {
+            const double r = pick_d((uint32_t)seq[k] & 3u, x, y, z, d);
+            k = (k + 1 == L) ? 0 : k + 1;
+            v = r * v * (1.0 - v);
+            double dd = r - 2.0 * r * v;
+            if (dd < 0) dd = -dd;
+            l += log(dd);
+            if ((((uint64_t)__double_as_longlong(l) >> 52) & 0x7ffu) == 0x7ffu)
+                return __longlong_as_double(0x7ff8000000000000ll);
+        }
+    } else {
+        l = ((double)e + log2(p)) * 0.693147180559945309417232121458176568;
+    }
+    return l / (double)si.A;
+}
+
 // --------------------------------------------------------------- the ray
 enum : uint32_t { PH_MARCH0 = 0, PH_MARCH = 1, PH_HONE = 2, PH_NORM0 = 3 };
 
@@ -489,6 +560,7 @@ struct Ray {
     V3 P, V, QdV, N;
     float t, t1, dt, Fdt, Ndt, a, c, l;
     float Qdt, Qt0, Qt1, minQdt, mag, lprev;
+    float tprev;   // t of the previous march sample (the bracket's far end)
     uint32_t phase, nm, nh, cap;
     bool near, sign;
 };
@@ -566,6 +638,7 @@ __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapP
     r.nh = 0;
     r.phase = PH_MARCH0;
     r.l = 0.0f;
+    r.tprev = t0;
     return true;
 }
 
@@ -586,11 +659,14 @@ __device__ __forceinline__ V3 ray_sample_point(const Ray &r)
     return Q;
 }
 
-enum : int { RAY_CONTINUE = 0, RAY_HIT = 1, RAY_MISS = 2 };
+// RAY_BRACKET: the march crossed the surface and the caller asked for the
+// crossing bracket [tprev, t] instead of honing (the precision form bisects it
+// in FP64 afterwards).
+enum : int { RAY_CONTINUE = 0, RAY_HIT = 1, RAY_MISS = 2, RAY_BRACKET = 3 };
 
 // Feed one lambda sample to the ray (kernel.cu:318-473); the ray either asks
 // for its next sample (RAY_CONTINUE) or ends.
-__device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &prm)
+__device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &prm, bool bracket = false)
 {
     const float opaque = prm.opaqueThreshold;
     bool to_normal = false;
@@ -650,6 +726,7 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
                     jit = (float)(1.0 + (double)(jit * prm.jitter));
                 if (f_isfinite(jit)) step = r.dt * jit;
             }
+            r.tprev = r.t;
             r.t = r.t + step;
             r.P = r.P + r.V * step;
             if (r.t > r.t1) return RAY_MISS;
@@ -657,6 +734,7 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
             return RAY_CONTINUE;
         }
         if (r.t > r.t1) return RAY_MISS;
+        if (bracket) return RAY_BRACKET;
         // start honing (kernel.cu:402-416)
         r.sign = false;
         r.Qdt = r.dt * -0.5f;

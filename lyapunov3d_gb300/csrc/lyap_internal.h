@@ -14,6 +14,8 @@ namespace lyapgb {
 cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_counter,
                           unsigned long long *d_stats, uint32_t blocks_per_sm, uint32_t threads,
                           cudaStream_t stream);
+cudaError_t launch_bisect(const RenderJob &job, uint32_t mode, uint32_t halvings, unsigned long long *d_stats,
+                          cudaStream_t stream);
 cudaError_t launch_volume(const VolumeJob &job, uint32_t mode, unsigned long long *d_stats,
                           uint32_t blocks_per_sm, uint32_t threads, cudaStream_t stream);
 

@@ -21,7 +21,11 @@ struct RenderJob {
     uint32_t n_lights;
     uint32_t width, height;
     uint32_t light_model;        // LYAP_LIGHT_SPOT | LYAP_LIGHT_DIRECTIONAL
-    uint32_t flags;              // LYAP_FLAG_* (LYAP_FLAG_NO_SPECULATION is read here)
+    uint32_t flags;              // LYAP_FLAG_* (NO_SPECULATION and BISECT_F64 are read here)
+    // LYAP_FLAG_BISECT_F64 only: the march stops at the crossing and records
+    // it; a second pass bisects it in double (lyap_precise.cu)
+    float *bracket;              // device, 2 per pixel: t of the last sample above, first at/below
+    uint32_t *hits;              // device, [0] = count, then the pixel indices that crossed
 };
 
 struct VolumeJob {

@@ -213,6 +213,7 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
     // march positions are known ahead only with a fixed step length
     const bool spec_ok = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f) &&
                          !(job.flags & LYAP_FLAG_NO_SPECULATION);
+    const bool bracket_mode = (job.flags & LYAP_FLAG_BISECT_F64) != 0u;
     LaneStats st = {};
     Ray r;
     r.phase = PH_MARCH0;
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
             st.samples += 1;
             st.skipped += skipped ? 1u : 0u;
             st.fallback += fallback ? 1u : 0u;
-            res = ray_advance(r, lam_v, job.prm);
+            res = ray_advance(r, lam_v, job.prm, bracket_mode);
         }
         if (ne) {
             const bool own_elig = (emask >> lane) & 1u;
@@ -336,11 +337,29 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
                     st.skipped += bj & 1u;
                     st.fallback += (bj >> 1) & 1u;
                     st.spec_used += 1;
-                    res = ray_advance(r, lj, job.prm);
+                    res = ray_advance(r, lj, job.prm, bracket_mode);
                 }
             }
         }
-        if (active && res != RAY_CONTINUE) {
+        if (active && res == RAY_BRACKET) {
+            // precision form: hand the crossing to the FP64 bisection pass
+            job.bracket[2 * (size_t)pix + 0] = r.tprev;
+            job.bracket[2 * (size_t)pix + 1] = r.t;
+            const uint32_t slot = atomicAdd(job.hits, 1u);
+            job.hits[1 + slot] = pix;
+            Ray keep = r;
+            keep.N = v3(0.f, 0.f, 0.f);
+            store_point(job.points + pix, keep, true);
+            reinterpret_cast<uint32_t *>(job.rgba)[pix] = 0u;
+            if (job.counts) {
+                job.counts[3 * (size_t)pix + 0] = r.nm;
+                job.counts[3 * (size_t)pix + 1] = 0u;
+                job.counts[3 * (size_t)pix + 2] = 0u;
+            }
+            st.march += r.nm;
+            st.rays += 1;
+            active = false;
+        } else if (active && res != RAY_CONTINUE) {
             finish_pixel(job.rgba, job.points, job.counts, pix, r, res == RAY_HIT, cr.C, job.lights, job.n_lights,
                          job.light_model, st);
             active = false;
