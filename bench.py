@@ -55,8 +55,9 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--volume", type=int, default=512, help="edge of the secondary volume sweep (0 = skip)")
     ap.add_argument("--no-jit", action="store_true", help="precompiled kernels only (no run-time specialisation)")
-    ap.add_argument("--report", choices=["precision"], default=None,
-                    help="instead of the benchmark, print the precision form's error report")
+    ap.add_argument("--report", choices=["precision", "batch"], default=None,
+                    help="instead of the benchmark, print the precision form's error report or time the batch")
+    ap.add_argument("--batch-scale", type=int, default=1, help="--report batch: divide every image side by this")
     return ap.parse_args()
 
 
@@ -485,10 +486,49 @@ def run_precision_report(args):
     print(json.dumps(report), flush=True)
 
 
+def run_batch_report(args):
+    """The batched workload (scenes.batch_workloads: 256 frames + 32 4-D slices,
+    sides divided by --batch-scale) as one autotuned, graph-captured launch,
+    product form: device time per launch, plain-method iterations per second,
+    the tuner's choice and candidate times."""
+    import torch
+    from lyapunov3d_gb300 import capi, scenes
+    from lyapunov3d_gb300.device import DeviceBatch
+    dev = torch.device("cuda", 0)
+    wls = scenes.batch_workloads(seed=4, scale=args.batch_scale)
+    t0 = time.perf_counter()
+    db = DeviceBatch(wls, device=dev, variant=capi.VARIANT_PRODUCT, autotune=True, counts=True)
+    t_create = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    db.run(stream)
+    torch.cuda.synchronize()
+    iters = db.iterations()
+    times = []
+    for _ in range(max(1, args.steps)):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        db.run(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    info = db.batch.info()
+    ms = statistics.mean(times)
+    print(json.dumps({
+        "report": "batch", "requests": len(wls), "pixels": sum(w.width * w.height for w in wls),
+        "scale": args.batch_scale, "create_s": t_create, "ms_per_launch": ms, "launch_ms": times,
+        "plain_iters_per_launch": iters, "g_iters_per_s": iters / (ms * 1e-3) / 1e9,
+        "tuned": {"tile": [info.tile_w, info.tile_h], "tiles_per_chunk": info.tiles_per_chunk,
+                  "blocks_per_sm": info.blocks_per_sm, "candidates_ms": list(info.tuned_ms)[:info.candidates]},
+        "chunks": info.chunks}), flush=True)
+
+
 def main():
     args = parse_args()
     if args.report == "precision":
         run_precision_report(args)
+        return
+    if args.report == "batch":
+        run_batch_report(args)
         return
     if args.impl == "reference":
         run_reference_arm(args)

@@ -323,6 +323,52 @@ int lyap_kernel_calc_render(uint32_t grid_x, uint32_t grid_y, uint32_t block_x, 
 int lyap_kernel_calc_volume(const uint32_t grid[3], const uint32_t block[3], float *d_exps,
                             const LyapParams *prm, int32_t *d_seq, void *stream);
 
+/* ---- batches: many renders in one launch -------------------------------
+ * No reference counterpart beyond kernel_calc_render itself: the reference
+ * renders one frame per launch (lyap_interactive.cu:711) and sweeps by
+ * re-running the program (scale.pl).  A batch holds requests of any image
+ * size, parameters, sequence (period <= LYAP_MAX_SEQ_LEN - 1) and light set;
+ * lyap_batch_create checks them, orders their tiles longest-job-first,
+ * optionally times candidate launch shapes on a sample of the batch (tile
+ * 32x1 / 8x4 / 16x16, 1 or 4 tiles per claim, 3 or 4 blocks per SM) and
+ * captures one CUDA graph that lyap_batch_run replays on any stream.  Each
+ * request's outputs are exactly what lyap_render gives for it. */
+typedef struct {
+    LyapCam cam;                  /* recalculated camera */
+    LyapParams prm;
+    const int32_t *d_seq;         /* device, seq_len entries incl. the -1 */
+    const LyapLight *d_lights;    /* device, recalculated */
+    RGBA *d_rgba;                 /* device, width*height */
+    LyapPoint *d_points;          /* device, width*height */
+    uint32_t *d_counts;           /* optional, 3 per pixel */
+    uint32_t seq_len, n_lights, width, height;
+    uint32_t light_model;         /* LYAP_LIGHT_* */
+    uint32_t flags;               /* LYAP_FLAG_NO_SPECULATION */
+} LyapRequest;
+
+typedef struct {
+    uint32_t size;                /* = sizeof(LyapBatchOptions) */
+    uint32_t variant;             /* LYAP_VARIANT_* for every request */
+    uint32_t autotune;            /* 1: time the candidate launch shapes */
+    uint32_t tile_w, tile_h, tiles_per_chunk, blocks_per_sm;   /* used when autotune = 0 */
+    uint32_t pad_;
+    unsigned long long *d_stats;  /* optional device LYAP_STAT_COUNT array */
+} LyapBatchOptions;
+
+typedef struct {
+    uint32_t size, requests, chunks;
+    uint32_t tile_w, tile_h, tiles_per_chunk, blocks_per_sm, threads_per_block;
+    uint32_t candidates, pad_;
+    float tuned_ms[16];           /* time of each candidate on the sample */
+} LyapBatchInfo;
+
+typedef struct LyapBatch LyapBatch;
+
+int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOptions *opt, LyapBatch **out);
+int lyap_batch_run(LyapBatch *batch, void *stream);
+int lyap_batch_info(const LyapBatch *batch, LyapBatchInfo *info);
+int lyap_batch_destroy(LyapBatch *batch);
+
 /* lyap4d (kernel.cu:108-154) at n arbitrary points: d_xyz holds x, y, z per
  * point (device, 3*n floats), symbol D takes prm->d; d_out receives n
  * lambdas in the form `form` (LYAP_VARIANT_PLAIN, LYAP_VARIANT_PRODUCT, or

@@ -64,6 +64,36 @@ class LyapRenderExt(ctypes.Structure):
             setattr(self, k, v)
 
 
+class LyapRequest(ctypes.Structure):
+    """One request of a batch (include/lyap_gb300.h)."""
+    _fields_ = [("cam", LyapCam), ("prm", LyapParams), ("d_seq", c_void_p), ("d_lights", c_void_p),
+                ("d_rgba", c_void_p), ("d_points", c_void_p), ("d_counts", c_void_p), ("seq_len", c_uint32),
+                ("n_lights", c_uint32), ("width", c_uint32), ("height", c_uint32), ("light_model", c_uint32),
+                ("flags", c_uint32), ("_pad_tail", ctypes.c_uint8 * 8)]   # C pads to LyapCam's 16-byte alignment
+
+
+assert ctypes.sizeof(LyapRequest) == 352
+
+
+class LyapBatchOptions(ctypes.Structure):
+    _fields_ = [("size", c_uint32), ("variant", c_uint32), ("autotune", c_uint32), ("tile_w", c_uint32),
+                ("tile_h", c_uint32), ("tiles_per_chunk", c_uint32), ("blocks_per_sm", c_uint32),
+                ("pad_", c_uint32), ("d_stats", c_void_p)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.size = ctypes.sizeof(LyapBatchOptions)
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+class LyapBatchInfo(ctypes.Structure):
+    _fields_ = [("size", c_uint32), ("requests", c_uint32), ("chunks", c_uint32), ("tile_w", c_uint32),
+                ("tile_h", c_uint32), ("tiles_per_chunk", c_uint32), ("blocks_per_sm", c_uint32),
+                ("threads_per_block", c_uint32), ("candidates", c_uint32), ("pad_", c_uint32),
+                ("tuned_ms", ctypes.c_float * 16)]
+
+
 class LyapVolumeExt(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("variant", c_uint32), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
                 ("threads_per_block", c_uint32), ("flags", c_uint32), ("pad_", c_uint32), ("h_seq", c_void_p)]
@@ -80,7 +110,7 @@ EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_
             "lyap_seq_parse", "lyap_cam_recalculate", "lyap_lights_recalculate", "lyap_render",
             "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
             "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc", "lyap_jit_info",
-            "lyap_lambda_points"]
+            "lyap_lambda_points", "lyap_batch_create", "lyap_batch_run", "lyap_batch_info", "lyap_batch_destroy"]
 
 
 def _load():
@@ -110,6 +140,10 @@ def _load():
     L.lyap_pipe_probe.argtypes = [c_uint32, c_uint32, c_void_p, POINTER(ctypes.c_double), c_void_p]
     L.lyap_jit_info.argtypes = [ctypes.c_char_p, c_size_t]
     L.lyap_lambda_points.argtypes = [c_void_p, c_size_t, c_void_p, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p]
+    L.lyap_batch_create.argtypes = [c_void_p, c_uint32, c_void_p, POINTER(c_void_p)]
+    L.lyap_batch_run.argtypes = [c_void_p, c_void_p]
+    L.lyap_batch_info.argtypes = [c_void_p, c_void_p]
+    L.lyap_batch_destroy.argtypes = [c_void_p]
     for name in EXPORTED:
         if name not in ("lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string"):
             getattr(L, name).restype = c_int
@@ -227,6 +261,38 @@ def lambda_points(d_xyz, n, prm, d_seq, seq_len, form, d_out, stream=None):
     """lyap_lambda_points: lambda at n points (x, y, z per point) in the given form."""
     _check(lib.lyap_lambda_points(_vp(d_xyz), n, ctypes.byref(prm), _vp(d_seq), seq_len, form, _vp(d_out),
                                   _stream(stream)))
+
+
+class Batch:
+    """A batch of render requests captured in one CUDA graph (lyap_batch_*)."""
+
+    def __init__(self, requests, variant=VARIANT_PLAIN, autotune=True, d_stats=None, **shape):
+        arr = (LyapRequest * len(requests))(*requests)
+        opt = LyapBatchOptions(variant=variant, autotune=1 if autotune else 0,
+                               d_stats=d_stats.data_ptr() if hasattr(d_stats, "data_ptr") else d_stats, **shape)
+        h = c_void_p()
+        _check(lib.lyap_batch_create(arr, len(requests), ctypes.byref(opt), ctypes.byref(h)))
+        self.handle = h
+        self._keep = (arr, opt)
+
+    def run(self, stream=None):
+        _check(lib.lyap_batch_run(self.handle, _stream(stream)))
+
+    def info(self):
+        i = LyapBatchInfo()
+        _check(lib.lyap_batch_info(self.handle, ctypes.byref(i)))
+        return i
+
+    def close(self):
+        if self.handle:
+            lib.lyap_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def pipe_probe(kind, iters, d_sink, stream=None):

@@ -201,6 +201,112 @@ __device__ __forceinline__ void flush_stats(unsigned long long *stats, const Lan
 }
 
 // ----------------------------------------------------------------- render
+// One round of the render loop for a warp: every lane evaluates one lambda
+// sample -- its own ray's next one, or, when the lane has no ray and
+// speculation is allowed, a sample ahead on a ray still running in the warp --
+// and the rays consume their results.  Returns the lane's ray outcome
+// (RAY_CONTINUE while it needs more samples).
+//
+// Speculation in the tail.  Once the queue is empty, lanes without a ray
+// evaluate, for the rays still running in this warp, the samples those rays
+// will ask for next.  That is only possible where the next positions do not
+// depend on the lambdas still to come: march steps when the step length is
+// fixed (no jitter, near multiplier 1), and the six normal samples.  Helper
+// lane (owner, j) takes the owner's j-th sample ahead; the owner feeds the
+// results to its state machine in order and drops the rest once the ray
+// leaves that phase.
+template <class Lam>
+__device__ __forceinline__ int sample_round(Ray &r, const bool active, const uint32_t amask, const Lam &lam,
+                                            const LyapParams &prm, const bool spec_ok, const bool bracket_mode,
+                                            LaneStats &st)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
+    bool helper = false;
+    uint32_t owner = lane, offset = 0;
+    if (spec_ok && amask != FULL) {
+        const bool elig = active && (r.phase <= PH_MARCH || (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5));
+        emask = __ballot_sync(FULL, elig);
+        ne = __popc(emask);
+        if (ne) {
+            imask = ~amask;
+            ni = __popc(imask);
+            maxj = (ni + ne - 1) / ne;
+            if (!active) {
+                const uint32_t rank = __popc(imask & ((1u << lane) - 1u));
+                owner = nth_set_bit(emask, rank % ne);
+                offset = 1 + rank / ne;
+                helper = true;
+            }
+        }
+    }
+    V3 Q = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
+    if (ne) {
+        // every lane reads its owner's state (its own, for non-helpers)
+        V3 oP, oV;
+        oP.x = __shfl_sync(FULL, r.P.x, owner);
+        oP.y = __shfl_sync(FULL, r.P.y, owner);
+        oP.z = __shfl_sync(FULL, r.P.z, owner);
+        oV.x = __shfl_sync(FULL, r.V.x, owner);
+        oV.y = __shfl_sync(FULL, r.V.y, owner);
+        oV.z = __shfl_sync(FULL, r.V.z, owner);
+        const float odt = __shfl_sync(FULL, r.dt, owner);
+        const float omag = __shfl_sync(FULL, r.mag, owner);
+        const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
+        if (helper) {
+            if (ophase <= PH_MARCH) {
+                // the position after `offset` more fixed steps, added one by one as ray_advance does
+                for (uint32_t j = 0; j < offset; j++) oP = oP + oV * odt;
+                Q = oP;
+            } else {
+                Ray tmp;
+                tmp.P = oP;
+                tmp.mag = omag;
+                const uint32_t k = ophase - PH_NORM0 + offset;
+                tmp.phase = PH_NORM0 + (k > 5 ? 5 : k);
+                Q = ray_sample_point(tmp);
+            }
+            st.spec += 1;
+        }
+    }
+
+    // one lambda sample for every lane (idle lanes evaluate a dummy point)
+    st.rounds += 1;
+    st.lane_rounds += __popc(amask) + (ne ? (ni < maxj * ne ? ni : maxj * ne) : 0u);
+    bool skipped, fallback;
+    const float lam_v = lam(Q.x, Q.y, Q.z, skipped, fallback);
+    int res = RAY_CONTINUE;
+    uint32_t kind = 0;   // 1: march, 2: normal
+    if (active) {
+        kind = (r.phase <= PH_MARCH) ? 1u : (r.phase >= PH_NORM0 ? 2u : 0u);
+        st.samples += 1;
+        st.skipped += skipped ? 1u : 0u;
+        st.fallback += fallback ? 1u : 0u;
+        res = ray_advance(r, lam_v, prm, bracket_mode);
+    }
+    if (ne) {
+        const bool own_elig = (emask >> lane) & 1u;
+        const uint32_t idx = __popc(emask & ((1u << lane) - 1u));
+        const uint32_t sk_bits = (skipped ? 1u : 0u) | (fallback ? 2u : 0u);
+        for (uint32_t j = 1; j <= maxj; j++) {
+            const uint32_t rr = (j - 1) * ne + idx;
+            const bool have = own_elig && rr < ni;
+            const uint32_t src = have ? nth_set_bit(imask, rr) : lane;
+            const float lj = __shfl_sync(FULL, lam_v, src);
+            const uint32_t bj = __shfl_sync(FULL, sk_bits, src);
+            const bool same_phase = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
+            if (have && res == RAY_CONTINUE && same_phase) {
+                st.samples += 1;
+                st.skipped += bj & 1u;
+                st.fallback += (bj >> 1) & 1u;
+                st.spec_used += 1;
+                res = ray_advance(r, lj, prm, bracket_mode);
+            }
+        }
+    }
+    return res;
+}
+
 template <class Lam>
 __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
     render_persistent(const __grid_constant__ RenderJob job, uint32_t *__restrict__ work_counter,
@@ -250,97 +356,7 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
         const uint32_t amask = __ballot_sync(FULL, active);
         if (amask == 0) break;
 
-        // Speculation in the tail.  Once the queue is empty, lanes without a
-        // ray evaluate, for the rays still running in this warp, the samples
-        // those rays will ask for next.  That is only possible where the next
-        // positions do not depend on the lambdas still to come: march steps
-        // when the step length is fixed (no jitter, near multiplier 1), and
-        // the six normal samples.  Helper lane (owner, j) takes the owner's
-        // j-th sample ahead; the owner feeds the results to its state machine
-        // in order and drops the rest once the ray leaves that phase.
-        uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
-        bool helper = false;
-        uint32_t owner = lane, offset = 0;
-        if (spec_ok && amask != FULL) {
-            const bool elig = active && (r.phase <= PH_MARCH || (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5));
-            emask = __ballot_sync(FULL, elig);
-            ne = __popc(emask);
-            if (ne) {
-                imask = ~amask;
-                ni = __popc(imask);
-                maxj = (ni + ne - 1) / ne;
-                if (!active) {
-                    const uint32_t rank = __popc(imask & ((1u << lane) - 1u));
-                    owner = nth_set_bit(emask, rank % ne);
-                    offset = 1 + rank / ne;
-                    helper = true;
-                }
-            }
-        }
-        V3 Q = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
-        if (ne) {
-            // every lane reads its owner's state (its own, for non-helpers)
-            V3 oP, oV;
-            oP.x = __shfl_sync(FULL, r.P.x, owner);
-            oP.y = __shfl_sync(FULL, r.P.y, owner);
-            oP.z = __shfl_sync(FULL, r.P.z, owner);
-            oV.x = __shfl_sync(FULL, r.V.x, owner);
-            oV.y = __shfl_sync(FULL, r.V.y, owner);
-            oV.z = __shfl_sync(FULL, r.V.z, owner);
-            const float odt = __shfl_sync(FULL, r.dt, owner);
-            const float omag = __shfl_sync(FULL, r.mag, owner);
-            const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
-            if (helper) {
-                if (ophase <= PH_MARCH) {
-                    // the position after `offset` more fixed steps, added one by one as ray_advance does
-                    for (uint32_t j = 0; j < offset; j++) oP = oP + oV * odt;
-                    Q = oP;
-                } else {
-                    Ray tmp;
-                    tmp.P = oP;
-                    tmp.mag = omag;
-                    const uint32_t k = ophase - PH_NORM0 + offset;
-                    tmp.phase = PH_NORM0 + (k > 5 ? 5 : k);
-                    Q = ray_sample_point(tmp);
-                }
-                st.spec += 1;
-            }
-        }
-
-        // one lambda sample for every lane (idle lanes evaluate a dummy point)
-        st.rounds += 1;
-        st.lane_rounds += __popc(amask) + (ne ? (ni < maxj * ne ? ni : maxj * ne) : 0u);
-        bool skipped, fallback;
-        const float lam_v = lam(Q.x, Q.y, Q.z, skipped, fallback);
-        int res = RAY_CONTINUE;
-        uint32_t kind = 0;   // 1: march, 2: normal
-        if (active) {
-            kind = (r.phase <= PH_MARCH) ? 1u : (r.phase >= PH_NORM0 ? 2u : 0u);
-            st.samples += 1;
-            st.skipped += skipped ? 1u : 0u;
-            st.fallback += fallback ? 1u : 0u;
-            res = ray_advance(r, lam_v, job.prm, bracket_mode);
-        }
-        if (ne) {
-            const bool own_elig = (emask >> lane) & 1u;
-            const uint32_t idx = __popc(emask & ((1u << lane) - 1u));
-            const uint32_t sk_bits = (skipped ? 1u : 0u) | (fallback ? 2u : 0u);
-            for (uint32_t j = 1; j <= maxj; j++) {
-                const uint32_t rr = (j - 1) * ne + idx;
-                const bool have = own_elig && rr < ni;
-                const uint32_t src = have ? nth_set_bit(imask, rr) : lane;
-                const float lj = __shfl_sync(FULL, lam_v, src);
-                const uint32_t bj = __shfl_sync(FULL, sk_bits, src);
-                const bool same_phase = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
-                if (have && res == RAY_CONTINUE && same_phase) {
-                    st.samples += 1;
-                    st.skipped += bj & 1u;
-                    st.fallback += (bj >> 1) & 1u;
-                    st.spec_used += 1;
-                    res = ray_advance(r, lj, job.prm, bracket_mode);
-                }
-            }
-        }
+        const int res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
         if (active && res == RAY_BRACKET) {
             // precision form: hand the crossing to the FP64 bisection pass
             job.bracket[2 * (size_t)pix + 0] = r.tprev;

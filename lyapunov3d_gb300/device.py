@@ -111,3 +111,44 @@ class DeviceVolume:
 
     def values(self):
         return self.d_out.cpu().numpy().reshape(self.nz, self.ny, self.nx)
+
+
+class DeviceBatch:
+    """A list of RenderWorkloads on the GPU as one lyap_batch (one graph launch)."""
+
+    def __init__(self, workloads, device="cuda", variant=capi.VARIANT_PLAIN, autotune=True, counts=False,
+                 **shape):
+        torch = _torch()
+        self.frames = [DeviceFrame(wl, device=device, counts=counts, stats=False) for wl in workloads]
+        self.d_stats = torch.zeros(capi.STAT_COUNT, dtype=torch.int64, device=device)
+        reqs = []
+        for f in self.frames:
+            q = capi.LyapRequest()
+            q.cam = f.cam
+            q.prm = f.prm
+            q.d_seq = f.d_seq.data_ptr()
+            q.d_lights = f.d_lights.data_ptr()
+            q.d_rgba = f.d_rgba.data_ptr()
+            q.d_points = f.d_points.data_ptr()
+            q.d_counts = f.d_counts.data_ptr() if f.d_counts is not None else None
+            q.seq_len = f.seq.size
+            q.n_lights = len(f.lights)
+            q.width, q.height = f.width, f.height
+            q.light_model = f.light_model
+            reqs.append(q)
+        self.batch = capi.Batch(reqs, variant=variant, autotune=autotune, d_stats=self.d_stats, **shape)
+
+    def run(self, stream=None):
+        self.batch.run(stream)
+
+    def stats(self):
+        return self.d_stats.cpu().numpy().astype(np.int64)
+
+    def iterations(self):
+        """Plain-method logistic iterations of one run, from the per-pixel sample
+        counts (requests differ in settle + accum; needs counts=True)."""
+        total = 0
+        for f in self.frames:
+            samples = int(f.d_counts.view(-1, 3).sum(dim=1, dtype=_torch().int64).sum().item())
+            total += samples * (f.prm.settle + f.prm.accum)
+        return total

@@ -197,3 +197,37 @@ def full_volume(n=512, seed=1):
     prm = make_params(200, 1000, lmin=2.0, lmax=4.0)
     return VolumeWorkload(f"volume{n}_seq12_200+1000_seed{seed}", (n, n, n), (2.0, 2.0, 2.0),
                           (4.0, 4.0, 4.0), seq, prm)
+
+
+def batch_workloads(seed=4, scale=1, n_render=256, n_slices=32):
+    """The batched workload: n_render frames with resolution drawn from
+    {256^2, 512^2, 1024^2, 1920x1080} (each side divided by `scale`), 128-1024
+    steps per ray, 200 settle + 200-4000 accumulated iterations (log-uniform),
+    sequences of length 2-16 over {A, B, C}; plus n_slices 4-D slices: the
+    same kind of frame with sequences over {A, B, C, D} and D uniform in
+    [2.5, 4].  Cameras orbit the [2, 4]^3 box at distance 5-8; thresholds are
+    the reference's defaults."""
+    rng = SplitMix64(0x4C594150_BA7C0000 | seed)
+    sizes = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
+    out = []
+    for i in range(n_render + n_slices):
+        w, h = sizes[rng.randint(4)]
+        w, h = max(1, w // scale), max(1, h // scale)
+        depth = float(128 + rng.randint(1024 - 128 + 1))
+        accum = int(round(math.exp(rng.uniform(math.log(200.0), math.log(4000.0)))))
+        L = 2 + rng.randint(15)
+        slice4d = i >= n_render
+        seq = random_sequence(rng, L, "ABCD" if slice4d else "ABC")
+        if slice4d and "D" not in seq:
+            seq = seq[:-1] + "D"
+        d = rng.uniform(2.5, 4.0) if slice4d else 2.1
+        q = uniform_quaternion(rng)
+        dist = rng.uniform(5.0, 8.0)
+        cam = orbit_camera(q, (3.0, 3.0, 3.0), dist)
+        prm = make_params(200, accum, d=d, step_method=1, depth=depth, opaque=-0.75, near=-1.0, near_mul=1.0,
+                          chaos=-0.5, jitter=0.0, refine=32.0, gradient=0.01, lmin=2.0, lmax=4.0)
+        light = headlight(cam, ambient=(0.08, 0.08, 0.08, 1.0))
+        kind = "slice" if slice4d else "frame"
+        out.append(RenderWorkload(f"batch{seed}_{i}_{kind}_{w}x{h}_{seq}_{accum}", w, h, seq, prm, cam, [light],
+                                  light_model=1))
+    return out

@@ -169,3 +169,34 @@ def test_drop_in_launcher_argument_errors():
     b = (ctypes.c_uint32 * 3)(8, 8, 8)
     assert L.lyap_kernel_calc_volume(g, b, ctypes.c_void_p(8), ctypes.byref(prm), ctypes.c_void_p(8), None) == \
         capi.LYAP_ERR_INVALID_ARG
+
+
+def test_abi_struct_sizes_match_c(tmp_path):
+    """Every struct of include/lyap_gb300.h has the same size and field offsets
+    in C (compiled here with gcc) as in the ctypes mirrors."""
+    import shutil
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    checks = {
+        "LyapRenderExt": (capi.LyapRenderExt, ["size", "flags", "d_counts", "d_stats", "h_seq", "bisect_halvings"]),
+        "LyapVolumeExt": (capi.LyapVolumeExt, ["variant", "d_stats", "flags", "h_seq"]),
+        "LyapRequest": (capi.LyapRequest, ["prm", "d_seq", "d_counts", "seq_len", "flags"]),
+        "LyapBatchOptions": (capi.LyapBatchOptions, ["autotune", "d_stats"]),
+        "LyapBatchInfo": (capi.LyapBatchInfo, ["candidates", "tuned_ms"]),
+    }
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "lyap_gb300.h"', "int main(void) {"]
+    for name, (_, fields) in checks.items():
+        src.append(f'printf("{name} size %zu\\n", sizeof({name}));')
+        for f in fields:
+            src.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    src.append("return 0; }")
+    c = tmp_path / "sizes.c"
+    c.write_text("\n".join(src))
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-std=c11", f"-I{os.path.join(ROOT, 'include')}", str(c), "-o", str(exe)], check=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                         check=True).stdout.splitlines())
+    for name, (cls, fields) in checks.items():
+        assert int(out[f"{name} size"]) == ctypes.sizeof(cls), name
+        for f in fields:
+            assert int(out[f"{name}.{f}"]) == getattr(cls, f).offset, (name, f)
