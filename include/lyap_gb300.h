@@ -214,7 +214,12 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_STAT_ROUNDS   10 /* render: warp rounds (one lambda sample each) */
 #define LYAP_STAT_LANE_ROUNDS 11 /* render: lanes sampling, summed over rounds */
 #define LYAP_STAT_MAX_ROUNDS 12  /* render: most rounds of any warp (max)     */
-#define LYAP_STAT_COUNT    13
+#define LYAP_STAT_PROPOSAL_SKIPPED 13 /* render: march samples the learned
+                                          proposal skipped (not evaluated) */
+#define LYAP_STAT_PROPOSAL_POINTS 14  /* render: points the proposal net evaluated */
+#define LYAP_STAT_NET_TIMEOUTS 15     /* tensor-core waits that ran out; the
+                                          tiles concerned skip nothing */
+#define LYAP_STAT_COUNT    16
 
 /* LyapRenderExt / LyapVolumeExt flags.  Given the host copy of the sequence
  * (h_seq), the library compiles the kernels for that sequence at run time
@@ -246,6 +251,19 @@ typedef struct {
     const int32_t *h_seq;        /* optional host copy of d_seq (seq_len entries) */
     uint32_t bisect_halvings;    /* LYAP_FLAG_BISECT_F64: halvings (0 = 20) */
     uint32_t pad_;
+    /* learned proposal (no reference counterpart): with a trained net
+     * (lyap_net_train), the march skips every segment of proposal_segment
+     * samples whose predicted lambda is >= opaqueThreshold + proposal_margin
+     * (with proposal_dilate, the neighbouring segments' predictions too).
+     * Every evaluated sample, hence every hit, is exact; a skipped segment
+     * adds nothing to the point's a and c sums.  Needs jitter 0 and
+     * nearMultiplier 1.  Callers built against the shorter struct (size =
+     * offsetof(LyapRenderExt, proposal)) keep working. */
+    const struct LyapNet *proposal; /* host struct, or NULL */
+    float proposal_margin;
+    uint32_t proposal_segment;   /* march samples per segment, 1..64 (0 = 8) */
+    uint32_t proposal_dilate;    /* 0 or 1 */
+    uint32_t pad2_;
 } LyapRenderExt;
 
 typedef struct {
@@ -258,6 +276,49 @@ typedef struct {
     uint32_t pad_;
     const int32_t *h_seq;        /* optional host copy of d_seq */
 } LyapVolumeExt;
+
+/* ---- learned proposal (no reference counterpart) ------------------------
+ * A Fourier-feature MLP over the parameter box predicts lambda, so that the
+ * march can skip segments the net calls empty (LyapRenderExt.proposal):
+ *   u = (P - lo) / (hi - lo);  f = 48 features sin(pi 2^k u_j), cos(pi 2^k u_j)
+ *   (k = 0..7, j = 0..2, feature 2*(3k+j) the sine, 2*(3k+j)+1 the cosine);
+ *   h1 = gelu(W1 f + b1), h2 = gelu(W2 h1 + b2) (64 each), lambda = w3.h2 + b3;
+ *   gelu(x) = x/2 (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))).
+ * The two matrix products run on the tensor cores with BF16 operands (f, W1,
+ * h1, W2 rounded to nearest-even BF16) and FP32 accumulation; w3 is rounded
+ * to BF16 as well, biases and h2 stay FP32.  params holds the FP32 master
+ * values: w1[64][48] (row = output), b1[64], w2[64][64], b2[64], w3[64], b3. */
+#define LYAP_NET_MAGIC    0x4E50594Cu  /* "LYPN" */
+#define LYAP_NET_VERSION  1u
+#define LYAP_NET_FEATURES 48
+#define LYAP_NET_HIDDEN   64
+#define LYAP_NET_PARAMS   7361
+typedef struct LyapNet {
+    uint32_t magic;              /* LYAP_NET_MAGIC */
+    uint32_t version;            /* LYAP_NET_VERSION */
+    float lo[3], hi[3];          /* input box */
+    float params[LYAP_NET_PARAMS];
+    float train_mse;             /* mean batch loss over the last 100 steps */
+    float val_mse;               /* on the held-out samples */
+    uint32_t steps, batch, n_samples;
+    uint32_t seq_hash;           /* FNV-1a 32 of the sequence, settle, accum and d it was trained for */
+    uint64_t hash;               /* FNV-1a 64 of every byte before it */
+} LyapNet;
+
+/* Training set-up (lyap_net_train); zero fields take the defaults. */
+typedef struct {
+    uint32_t size;               /* = sizeof(LyapNetTrainOptions) */
+    uint32_t n_samples;          /* training samples (0 = 1 << 20) */
+    uint32_t n_val;              /* held-out samples (0 = 1 << 16) */
+    uint32_t batch;              /* samples per step, multiple of 128, <= 32768 (0 = 4096) */
+    uint32_t steps;              /* Adam steps (0 = 8192) */
+    float lr;                    /* peak learning rate, cosine decay to 0 (0 = 3e-3) */
+    float target_lo, target_hi;  /* lambda clamp; NaN counts as target_lo (both 0: -3, 1) */
+    uint64_t seed;
+    const float *box_lo;         /* host, 3 floats; NULL = (lMin, lMin, lMin) */
+    const float *box_hi;         /* host, 3 floats; NULL = (lMax, lMax, lMax) */
+    float *h_loss;               /* optional host array of `steps` floats: each step's batch loss */
+} LyapNetTrainOptions;
 
 #ifndef __CUDACC_RTC__   /* host entry points: not part of device-side compiles */
 /* ---- entry points ------------------------------------------------------ */
@@ -410,6 +471,29 @@ int lyap_jit_info(char *buf, size_t cap);
  * lg2.approx; *ops receives the operations performed.  The rate is the
  * denominator of the lambda kernels' FP32 / MUFU roofline. */
 int lyap_pipe_probe(uint32_t kind, uint32_t iters, float *d_sink, double *ops, void *stream);
+
+/* ---- learned proposal entry points (no reference counterpart) ----------- */
+/* Trains `net` on the GPU: n_samples + n_val points uniform in the box,
+ * lambda at each by the plain FP32 method for this sequence and parameters
+ * (the drop-in's own lyap4d), clamped; then `steps` Adam steps of mean
+ * squared error on random batches, each a forward and backward pass on the
+ * tensor cores.  seq is a host array (seq_len entries incl. the -1).
+ * Deterministic for a given seed.  Returns after the stream is synchronised. */
+int lyap_net_train(const LyapParams *prm, const int32_t *seq, size_t seq_len, const LyapNetTrainOptions *opt,
+                   LyapNet *net, void *stream);
+/* The net at n points (d_xyz: 3 floats per point, device) into d_out[n]
+ * (device), on the tensor cores.  Asynchronous. */
+int lyap_net_eval(const LyapNet *net, const float *d_xyz, size_t n, float *d_out, void *stream);
+/* Gradient of the loss (1/n) sum_i (net(x_i) - t_i)^2 with respect to
+ * params, by the training kernels (forward and backward on the tensor
+ * cores): d_grad receives LYAP_NET_PARAMS floats, d_loss (may be NULL) the
+ * loss.  n is a multiple of 128, at most 32768.  Asynchronous. */
+int lyap_net_grad(const LyapNet *net, const float *d_xyz, const float *d_target, size_t n, float *d_grad,
+                  float *d_loss, void *stream);
+/* The net as a file (the struct's bytes) and back; load checks magic,
+ * version and hash. */
+int lyap_net_save(const LyapNet *net, const char *path);
+int lyap_net_load(LyapNet *net, const char *path);
 
 #endif /* !__CUDACC_RTC__ */
 

@@ -24,9 +24,10 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "liblyap_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["lyap_render.cu", "lyap_volume.cu", "lyap_capi.cu", "lyap_probe.cu", "lyap_noalloc.cu", "lyap_precise.cu", "lyap_batch.cu"]
+CUDA_SOURCES = ["lyap_render.cu", "lyap_volume.cu", "lyap_capi.cu", "lyap_probe.cu", "lyap_noalloc.cu", "lyap_precise.cu", "lyap_batch.cu", "lyap_net.cu"]
 CXX_SOURCES = ["lyap_scene.cpp", "lyap_jit.cpp"]
-HEADERS = ["lyap_device.cuh", "lyap_internal.h", "lyap_jobs.h", "lyap_kernels.cuh", "lyap_jit.h"]
+HEADERS = ["lyap_device.cuh", "lyap_internal.h", "lyap_jobs.h", "lyap_kernels.cuh", "lyap_jit.h", "lyap_net.cuh",
+           "lyap_tc.cuh"]
 # headers NVRTC compiles at run time (embedded into the library), and minimal
 # stand-ins for the two C headers they include
 JIT_HEADERS = [("lyap_gb300.h", "INCLUDE"), ("lyap_jobs.h", "CSRC"), ("lyap_device.cuh", "CSRC"),

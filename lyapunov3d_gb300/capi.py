@@ -40,8 +40,15 @@ MAX_SEQ_LEN = 4096
 MAX_LIGHTS = 16
 
 (STAT_SAMPLES, STAT_SKIPPED, STAT_MARCH, STAT_HONE, STAT_NORMAL, STAT_HITS, STAT_RAYS, STAT_FALLBACK, STAT_SPEC,
- STAT_SPEC_USED, STAT_ROUNDS, STAT_LANE_ROUNDS, STAT_MAX_ROUNDS) = range(13)
-STAT_COUNT = 13
+ STAT_SPEC_USED, STAT_ROUNDS, STAT_LANE_ROUNDS, STAT_MAX_ROUNDS, STAT_PROPOSAL_SKIPPED, STAT_PROPOSAL_POINTS,
+ STAT_NET_TIMEOUTS) = range(16)
+STAT_COUNT = 16
+
+NET_MAGIC = 0x4E50594C
+NET_VERSION = 1
+NET_FEATURES = 48
+NET_HIDDEN = 64
+NET_PARAMS = 7361
 
 
 class LyapError(RuntimeError):
@@ -51,11 +58,35 @@ class LyapError(RuntimeError):
         self.message = message
 
 
+class LyapNet(ctypes.Structure):
+    """The learned proposal's network (include/lyap_gb300.h)."""
+    _fields_ = [("magic", c_uint32), ("version", c_uint32), ("lo", c_float * 3), ("hi", c_float * 3),
+                ("params", c_float * NET_PARAMS), ("train_mse", c_float), ("val_mse", c_float),
+                ("steps", c_uint32), ("batch", c_uint32), ("n_samples", c_uint32), ("seq_hash", c_uint32),
+                ("hash", ctypes.c_uint64)]
+
+    def param_array(self):
+        return np.ctypeslib.as_array(self.params).astype(np.float64)
+
+
+class LyapNetTrainOptions(ctypes.Structure):
+    _fields_ = [("size", c_uint32), ("n_samples", c_uint32), ("n_val", c_uint32), ("batch", c_uint32),
+                ("steps", c_uint32), ("lr", c_float), ("target_lo", c_float), ("target_hi", c_float),
+                ("seed", ctypes.c_uint64), ("box_lo", c_void_p), ("box_hi", c_void_p), ("h_loss", c_void_p)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.size = ctypes.sizeof(LyapNetTrainOptions)
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
 class LyapRenderExt(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("variant", c_uint32), ("light_model", c_uint32), ("flags", c_uint32),
                 ("d_counts", c_void_p), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
                 ("threads_per_block", c_uint32), ("h_seq", c_void_p), ("bisect_halvings", c_uint32),
-                ("pad_", c_uint32)]
+                ("pad_", c_uint32), ("proposal", POINTER(LyapNet)), ("proposal_margin", c_float),
+                ("proposal_segment", c_uint32), ("proposal_dilate", c_uint32), ("pad2_", c_uint32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -110,7 +141,8 @@ EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_
             "lyap_seq_parse", "lyap_cam_recalculate", "lyap_lights_recalculate", "lyap_render",
             "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
             "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc", "lyap_jit_info",
-            "lyap_lambda_points", "lyap_batch_create", "lyap_batch_run", "lyap_batch_info", "lyap_batch_destroy"]
+            "lyap_lambda_points", "lyap_batch_create", "lyap_batch_run", "lyap_batch_info", "lyap_batch_destroy",
+            "lyap_net_train", "lyap_net_eval", "lyap_net_grad", "lyap_net_save", "lyap_net_load"]
 
 
 def _load():
@@ -144,6 +176,11 @@ def _load():
     L.lyap_batch_run.argtypes = [c_void_p, c_void_p]
     L.lyap_batch_info.argtypes = [c_void_p, c_void_p]
     L.lyap_batch_destroy.argtypes = [c_void_p]
+    L.lyap_net_train.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
+    L.lyap_net_eval.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p]
+    L.lyap_net_grad.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
+    L.lyap_net_save.argtypes = [c_void_p, c_char_p]
+    L.lyap_net_load.argtypes = [c_void_p, c_char_p]
     for name in EXPORTED:
         if name not in ("lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string"):
             getattr(L, name).restype = c_int
@@ -326,3 +363,61 @@ def volume_host(nx, ny, nz, prm, seq, lo=None, hi=None, ext=None, stream=None, o
     _check(lib.lyap_volume_host(_vp(out), nx, ny, nz, lo_a, hi_a, ctypes.byref(prm), _vp(seq), seq.size,
                                 ctypes.byref(ext) if ext is not None else None, _stream(stream)))
     return out
+
+
+# ---- learned proposal ------------------------------------------------------
+def net_train(prm, seq, stream=None, box_lo=None, box_hi=None, with_loss=False, **opts):
+    """lyap_net_train: a LyapNet trained on the GPU for this sequence and
+    params (options as LyapNetTrainOptions fields); with_loss also returns
+    each step's batch loss."""
+    seq = np.ascontiguousarray(seq, dtype=np.int32)
+    lo = (c_float * 3)(*box_lo) if box_lo is not None else None
+    hi = (c_float * 3)(*box_hi) if box_hi is not None else None
+    o = LyapNetTrainOptions(**opts)
+    if lo is not None:
+        o.box_lo = ctypes.cast(lo, c_void_p)
+    if hi is not None:
+        o.box_hi = ctypes.cast(hi, c_void_p)
+    steps = o.steps or 8192
+    loss = np.zeros(steps, dtype=np.float32) if with_loss else None
+    if loss is not None:
+        o.h_loss = loss.ctypes.data
+    net = LyapNet()
+    _check(lib.lyap_net_train(ctypes.byref(prm), _vp(seq), seq.size, ctypes.byref(o), ctypes.byref(net),
+                              _stream(stream)))
+    return (net, loss) if with_loss else net
+
+
+def net_eval(net, d_xyz, n, d_out, stream=None):
+    """lyap_net_eval: the net at n device points (3 floats each) into d_out."""
+    _check(lib.lyap_net_eval(ctypes.byref(net), _vp(d_xyz), n, _vp(d_out), _stream(stream)))
+
+
+def net_grad(net, d_xyz, d_target, n, d_grad, d_loss=None, stream=None):
+    """lyap_net_grad: d(mean squared error)/d(params) into d_grad (NET_PARAMS floats)."""
+    _check(lib.lyap_net_grad(ctypes.byref(net), _vp(d_xyz), _vp(d_target), n, _vp(d_grad), _vp(d_loss),
+                             _stream(stream)))
+
+
+def net_save(net, path):
+    _check(lib.lyap_net_save(ctypes.byref(net), os.fsencode(path)))
+
+
+def net_load(path):
+    net = LyapNet()
+    _check(lib.lyap_net_load(ctypes.byref(net), os.fsencode(path)))
+    return net
+
+
+def net_from_params(params, lo, hi):
+    """A LyapNet with the given FP32 parameters and input box (hash left to lyap_net_save)."""
+    net = LyapNet()
+    net.magic = NET_MAGIC
+    net.version = NET_VERSION
+    for k in range(3):
+        net.lo[k] = lo[k]
+        net.hi[k] = hi[k]
+    p = np.asarray(params, dtype=np.float32)
+    assert p.size == NET_PARAMS
+    ctypes.memmove(net.params, p.ctypes.data, p.nbytes)
+    return net

@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(128, 4) render_batch(const __grid_constant__ B
                     if (ray_init(r, cr, prm, x, y)) {
                         active = true;
                     } else {
-                        r.nm = r.nh = 0;
+                        r.nm = r.nh = r.ns = 0;
                         finish_pixel(J->rgba, J->points, J->counts, pix, r, false, cr.C, J->lights, J->n_lights,
                                      J->light_model, st);
                     }

@@ -5,7 +5,9 @@
 // lyap_last_error_string().
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -64,12 +66,35 @@ static int check_host_seq(const int32_t *seq, size_t seq_len, const char *fn)
     return LYAP_OK;
 }
 
-static int check_ext_render(const LyapRenderExt *ext, const char *fn)
+// the proposal fields exist only in the full-size struct
+const LyapNet *ext_proposal(const LyapRenderExt *ext)
+{
+    return (ext && ext->size == sizeof(LyapRenderExt)) ? ext->proposal : nullptr;
+}
+
+static int check_ext_render(const LyapRenderExt *ext, const LyapParams *prm, const char *fn)
 {
     if (!ext) return LYAP_OK;
-    if (ext->size != sizeof(LyapRenderExt))
-        return set_error(LYAP_ERR_INVALID_ARG, "%s: LyapRenderExt.size is %u, expected %zu", fn, ext->size,
-                         sizeof(LyapRenderExt));
+    if (ext->size != sizeof(LyapRenderExt) && ext->size != offsetof(LyapRenderExt, proposal))
+        return set_error(LYAP_ERR_INVALID_ARG, "%s: LyapRenderExt.size is %u, expected %zu (or %zu)", fn, ext->size,
+                         sizeof(LyapRenderExt), offsetof(LyapRenderExt, proposal));
+    if (const LyapNet *net = ext_proposal(ext)) {
+        if (net->magic != LYAP_NET_MAGIC || net->version != LYAP_NET_VERSION)
+            return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal is not a LyapNet (magic %08x, version %u)", fn,
+                             net->magic, net->version);
+        for (int k = 0; k < 3; k++)
+            if (!(net->hi[k] > net->lo[k]))
+                return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal net has an empty box on axis %d", fn, k);
+        if (!std::isfinite(ext->proposal_margin))
+            return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal_margin is not finite", fn);
+        if (ext->proposal_segment > 64)
+            return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal_segment %u > 64", fn, ext->proposal_segment);
+        if (ext->proposal_dilate > 1)
+            return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal_dilate must be 0 or 1", fn);
+        if (prm->jitter != 0.0f || prm->nearMultiplier != 1.0f)
+            return set_error(LYAP_ERR_INVALID_ARG,
+                             "%s: the proposal needs a fixed step (jitter 0, nearMultiplier 1)", fn);
+    }
     if (ext->variant > LYAP_VARIANT_PRODUCT) return set_error(LYAP_ERR_INVALID_ARG, "%s: unknown variant %u", fn, ext->variant);
     if (ext->light_model > LYAP_LIGHT_DIRECTIONAL)
         return set_error(LYAP_ERR_INVALID_ARG, "%s: unknown light model %u", fn, ext->light_model);
@@ -107,7 +132,7 @@ int check_render_args(const LyapCam *cam, const LyapParams *prm, const void *seq
     if ((uint64_t)width * height > LYAP_MAX_PIXELS)
         return set_error(LYAP_ERR_INVALID_ARG, "%s: %ux%u exceeds %llu pixels", fn, width, height,
                          (unsigned long long)LYAP_MAX_PIXELS);
-    return check_ext_render(ext, fn);
+    return check_ext_render(ext, prm, fn);
 }
 
 RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
@@ -172,10 +197,18 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     // on different streams each get their own
     // precision form with FP64 bisection: also the per-pixel crossing
     // brackets and the list of pixels that crossed (scratch of the two passes)
+    // learned proposal: the net, the crossing rays and the per-pixel segment bits
     const bool bisect = ext && (ext->flags & LYAP_FLAG_BISECT_F64);
     const size_t npix = (size_t)width * height;
-    const size_t scratch = bisect ? 256 + (npix + 1) * sizeof(uint32_t) + 256 + npix * 2 * sizeof(float)
-                                  : sizeof(uint32_t);
+    const LyapNet *net = ext_proposal(ext);
+    const uint32_t seg_len = net ? (ext->proposal_segment ? ext->proposal_segment : 8u) : 0u;
+    uint32_t words = 0;
+    if (net && proposal_segments(*prm, seg_len, &words) == 0) net = nullptr;
+    const size_t bisect_bytes = bisect ? 256 + (((npix + 1) * sizeof(uint32_t) + 255) & ~(size_t)255) +
+                                             npix * 2 * sizeof(float)
+                                       : sizeof(uint32_t);
+    const size_t prop_off = (bisect_bytes + 255) & ~(size_t)255;
+    const size_t scratch = net ? prop_off + proposal_scratch_bytes(npix, words) : bisect_bytes;
     uint32_t *d_counter = nullptr;
     cudaError_t e = cudaMallocAsync((void **)&d_counter, scratch, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: scratch allocation");
@@ -186,6 +219,9 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
         job.bracket = reinterpret_cast<float *>(base + 256 + (((npix + 1) * sizeof(uint32_t) + 255) & ~(size_t)255));
         e = cudaMemsetAsync(job.hits, 0, sizeof(uint32_t), s);
     }
+    if (e == cudaSuccess && net)
+        e = launch_proposal(job, *net, ext->proposal_margin, seg_len, ext->proposal_dilate,
+                            reinterpret_cast<char *>(d_counter) + prop_off, ext->d_stats, s);
     if (e == cudaSuccess) {
         const uint32_t variant = ext ? ext->variant : LYAP_VARIANT_PLAIN;
         const uint32_t flags = ext ? ext->flags : 0u;
@@ -288,12 +324,9 @@ int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *s
     if (e == cudaSuccess) {
         // the sequence is on the host here: hand it on for the specialised kernels
         LyapRenderExt x;
-        if (ext) {
-            x = *ext;
-        } else {
-            memset(&x, 0, sizeof(x));
-            x.size = sizeof(x);
-        }
+        memset(&x, 0, sizeof(x));
+        if (ext) memcpy(&x, ext, ext->size);   // a short (older) struct: the rest stays zero
+        x.size = sizeof(x);
         if (!x.h_seq) x.h_seq = seq;
         rc = lyap_render(cam, prm, (const int32_t *)dev, seq_len, (const LyapLight *)(dev + off_l), n_lights,
                          (RGBA *)(dev + off_r), (LyapPoint *)(dev + off_p), width, height, &x, stream);

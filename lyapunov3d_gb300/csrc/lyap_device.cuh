@@ -562,6 +562,7 @@ struct Ray {
     float Qdt, Qt0, Qt1, minQdt, mag, lprev;
     float tprev;   // t of the previous march sample (the bracket's far end)
     uint32_t phase, nm, nh, cap;
+    uint32_t ns;     // march samples the learned proposal skipped (counted in nm, never evaluated)
     bool near, sign;
 };
 
@@ -636,6 +637,7 @@ __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapP
     r.cap = (capd > 0.0 && capd < (double)MARCH_MAX) ? (uint32_t)capd : MARCH_MAX;
     r.nm = 0;
     r.nh = 0;
+    r.ns = 0;
     r.phase = PH_MARCH0;
     r.l = 0.0f;
     r.tprev = t0;

@@ -26,6 +26,14 @@ struct RenderJob {
     // it; a second pass bisects it in double (lyap_precise.cu)
     float *bracket;              // device, 2 per pixel: t of the last sample above, first at/below
     uint32_t *hits;              // device, [0] = count, then the pixel indices that crossed
+    // learned proposal: per pixel skip_words words of bits, bit j set when the
+    // net predicts lambda above the skip threshold for march segment j
+    // (samples j*seg_len .. j*seg_len + seg_len - 1); null = no proposal
+    const uint32_t *skip;
+    uint32_t skip_words;         // words per pixel
+    uint32_t skip_segments;      // segments covered by the bits (later samples are always evaluated)
+    uint32_t seg_len;            // march samples per segment
+    uint32_t skip_dilate;        // 1: a segment is skipped only if its neighbours' bits are set too
 };
 
 struct VolumeJob {

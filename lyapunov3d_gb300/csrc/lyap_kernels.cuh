@@ -125,6 +125,7 @@ struct ConstLambda {
 struct LaneStats {
     uint32_t samples, skipped, march, hone, normal, hits, rays, fallback, spec, spec_used;
     uint32_t rounds, lane_rounds;   // per warp, kept by every lane alike
+    uint32_t prop_skip;             // march samples skipped on the learned proposal's word
 };
 
 // position of the n-th (0-based) set bit of mask; mask has more than n bits set
@@ -170,11 +171,12 @@ __device__ __forceinline__ void finish_pixel(RGBA *rgba, LyapPoint *points, uint
     }
     reinterpret_cast<uint32_t *>(rgba)[ind] = px;
     if (counts) {
-        counts[3 * (size_t)ind + 0] = r.nm;
+        counts[3 * (size_t)ind + 0] = r.nm - r.ns;
         counts[3 * (size_t)ind + 1] = r.nh;
         counts[3 * (size_t)ind + 2] = hit ? 6u : 0u;
     }
-    st.march += r.nm;
+    st.march += r.nm - r.ns;
+    st.prop_skip += r.ns;
     st.hone += r.nh;
     st.normal += hit ? 6u : 0u;
     st.hits += hit ? 1u : 0u;
@@ -193,6 +195,8 @@ __device__ __forceinline__ void flush_stats(unsigned long long *stats, const Lan
         const uint32_t s = __reduce_add_sync(mask, v[k]);
         if (lane == leader && s) atomicAdd(stats + k, (unsigned long long)s);
     }
+    const uint32_t ps = __reduce_add_sync(mask, st.prop_skip);
+    if (lane == leader && ps) atomicAdd(stats + LYAP_STAT_PROPOSAL_SKIPPED, (unsigned long long)ps);
     if (lane == leader && st.rounds) {
         atomicAdd(stats + LYAP_STAT_ROUNDS, (unsigned long long)st.rounds);
         atomicAdd(stats + LYAP_STAT_LANE_ROUNDS, (unsigned long long)st.lane_rounds);
@@ -307,6 +311,44 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     return res;
 }
 
+// Learned proposal: at the start of every march segment the net marked empty
+// the ray takes the segment's steps without evaluating lambda.  Each step is
+// the one ray_advance takes after a sample above the opaque threshold (count
+// the sample, stop at the sample cap, advance t and P, stop past t1), so the
+// samples after a skip sit at exactly the positions the exact march visits.
+// Requires a fixed step length (no jitter, near multiplier 1).  Returns
+// RAY_MISS when the ray leaves the box while skipping.
+__device__ __forceinline__ bool proposal_bit(const uint32_t *row, uint32_t j)
+{
+    return (__ldg(row + (j >> 5)) >> (j & 31u)) & 1u;
+}
+
+__device__ __forceinline__ int proposal_skip(Ray &r, const RenderJob &job, uint32_t pix)
+{
+    const uint32_t G = job.seg_len;
+    const uint32_t *row = job.skip + (size_t)pix * job.skip_words;
+    for (;;) {
+        const uint32_t k = r.nm;
+        if (k % G != 0u) return RAY_CONTINUE;
+        const uint32_t j = k / G;
+        if (j >= job.skip_segments || !proposal_bit(row, j)) return RAY_CONTINUE;
+        if (job.skip_dilate) {
+            if (j > 0u && !proposal_bit(row, j - 1u)) return RAY_CONTINUE;
+            if (j + 1u < job.skip_segments && !proposal_bit(row, j + 1u)) return RAY_CONTINUE;
+        }
+        for (uint32_t s = 0; s < G; s++) {
+            r.nm += 1;
+            r.ns += 1;
+            if (r.nm >= r.cap) return RAY_MISS;
+            r.tprev = r.t;
+            r.t = r.t + r.dt;
+            r.P = r.P + r.V * r.dt;
+            if (r.t > r.t1) return RAY_MISS;
+        }
+        r.phase = PH_MARCH;
+    }
+}
+
 template <class Lam>
 __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
     render_persistent(const __grid_constant__ RenderJob job, uint32_t *__restrict__ work_counter,
@@ -317,8 +359,9 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
     const Lam lam(job.seq, job.seq_period, job.prm);
     const CamRays cr = cam_rays(job.cam);
     // march positions are known ahead only with a fixed step length
+    // (with a proposal the march positions depend on its skips: no speculation)
     const bool spec_ok = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f) &&
-                         !(job.flags & LYAP_FLAG_NO_SPECULATION);
+                         !(job.flags & LYAP_FLAG_NO_SPECULATION) && job.skip == nullptr;
     const bool bracket_mode = (job.flags & LYAP_FLAG_BISECT_F64) != 0u;
     LaneStats st = {};
     Ray r;
@@ -345,8 +388,13 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
                     const uint32_t sx = my % job.width, sy = my / job.width;
                     if (ray_init(r, cr, job.prm, sx, sy)) {
                         active = true;
+                        if (job.skip && proposal_skip(r, job, my) == RAY_MISS) {
+                            finish_pixel(job.rgba, job.points, job.counts, my, r, false, cr.C, job.lights,
+                                         job.n_lights, job.light_model, st);
+                            active = false;
+                        }
                     } else {
-                        r.nm = r.nh = 0;
+                        r.nm = r.nh = r.ns = 0;
                         finish_pixel(job.rgba, job.points, job.counts, my, r, false, cr.C, job.lights,
                                      job.n_lights, job.light_model, st);
                     }
@@ -356,7 +404,8 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
         const uint32_t amask = __ballot_sync(FULL, active);
         if (amask == 0) break;
 
-        const int res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
+        int res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
+        if (active && res == RAY_CONTINUE && job.skip && r.phase == PH_MARCH) res = proposal_skip(r, job, pix);
         if (active && res == RAY_BRACKET) {
             // precision form: hand the crossing to the FP64 bisection pass
             job.bracket[2 * (size_t)pix + 0] = r.tprev;
@@ -368,11 +417,12 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
             store_point(job.points + pix, keep, true);
             reinterpret_cast<uint32_t *>(job.rgba)[pix] = 0u;
             if (job.counts) {
-                job.counts[3 * (size_t)pix + 0] = r.nm;
+                job.counts[3 * (size_t)pix + 0] = r.nm - r.ns;
                 job.counts[3 * (size_t)pix + 1] = 0u;
                 job.counts[3 * (size_t)pix + 2] = 0u;
             }
-            st.march += r.nm;
+            st.march += r.nm - r.ns;
+            st.prop_skip += r.ns;
             st.rays += 1;
             active = false;
         } else if (active && res != RAY_CONTINUE) {

@@ -76,6 +76,9 @@ extern "C" int lyap_render_noalloc(const LyapCam *cam, const LyapParams *prm, co
     int rc = check_render_args(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext,
                                "lyap_render_noalloc");
     if (rc) return rc;
+    if (ext_proposal(ext))
+        return set_error(LYAP_ERR_INVALID_ARG, "lyap_render_noalloc: the learned proposal needs scratch memory; "
+                                               "use lyap_render");
     if (ext && (ext->flags & LYAP_FLAG_BISECT_F64))
         return set_error(LYAP_ERR_INVALID_ARG,
                          "lyap_render_noalloc: LYAP_FLAG_BISECT_F64 needs per-pixel scratch; use lyap_render");

@@ -95,7 +95,7 @@ LYAP_KERNEL_EXPORT __global__ void kernel_calc_render(RGBA *rgba, LyapPoint *poi
                     if (ray_init(r, cr, prm, x, y)) {
                         active = true;
                     } else {
-                        r.nm = r.nh = 0;
+                        r.nm = r.nh = r.ns = 0;
                         finish_pixel(rgba, points, nullptr, ind, r, false, cr.C, lights, num_lights,
                                      LYAP_LIGHT_SPOT, st);
                     }

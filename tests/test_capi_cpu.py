@@ -178,7 +178,10 @@ def test_abi_struct_sizes_match_c(tmp_path):
     if not shutil.which("gcc"):
         pytest.skip("gcc not available")
     checks = {
-        "LyapRenderExt": (capi.LyapRenderExt, ["size", "flags", "d_counts", "d_stats", "h_seq", "bisect_halvings"]),
+        "LyapRenderExt": (capi.LyapRenderExt, ["size", "flags", "d_counts", "d_stats", "h_seq", "bisect_halvings",
+                                               "proposal", "proposal_margin", "proposal_dilate", "pad2_"]),
+        "LyapNet": (capi.LyapNet, ["lo", "hi", "params", "train_mse", "val_mse", "seq_hash", "hash"]),
+        "LyapNetTrainOptions": (capi.LyapNetTrainOptions, ["steps", "lr", "seed", "box_lo", "box_hi", "h_loss"]),
         "LyapVolumeExt": (capi.LyapVolumeExt, ["variant", "d_stats", "flags", "h_seq"]),
         "LyapRequest": (capi.LyapRequest, ["prm", "d_seq", "d_counts", "seq_len", "flags"]),
         "LyapBatchOptions": (capi.LyapBatchOptions, ["autotune", "d_stats"]),
@@ -200,3 +203,79 @@ def test_abi_struct_sizes_match_c(tmp_path):
         assert int(out[f"{name} size"]) == ctypes.sizeof(cls), name
         for f in fields:
             assert int(out[f"{name}.{f}"]) == getattr(cls, f).offset, (name, f)
+
+
+def _net(seed=0):
+    rng = np.random.default_rng(seed)
+    return capi.net_from_params(rng.standard_normal(capi.NET_PARAMS) * 0.1, (2.0, 2.0, 2.0), (4.0, 4.0, 4.0))
+
+
+def test_net_save_load_roundtrip(tmp_path):
+    net = _net()
+    path = str(tmp_path / "net.bin")
+    capi.net_save(net, path)
+    back = capi.net_load(path)
+    assert bytes(back)[:-8] == bytes(net)[:-8]
+    assert back.hash != 0
+    # a flipped byte in the weights, a truncated file and a foreign file are refused
+    raw = bytearray(open(path, "rb").read())
+    raw[100] ^= 1
+    open(path, "wb").write(bytes(raw))
+    with pytest.raises(capi.LyapError, match="hash mismatch"):
+        capi.net_load(path)
+    open(path, "wb").write(bytes(raw[:-1]))
+    with pytest.raises(capi.LyapError, match="not"):
+        capi.net_load(path)
+    open(path, "wb").write(b"\0" * ctypes.sizeof(capi.LyapNet))
+    with pytest.raises(capi.LyapError, match="not a LyapNet"):
+        capi.net_load(path)
+
+
+@pytest.mark.parametrize("change,msg", [
+    (dict(magic=0), "not a LyapNet"),
+    (dict(segment=65), "proposal_segment"),
+    (dict(dilate=2), "proposal_dilate"),
+    (dict(margin=float("nan")), "proposal_margin"),
+    (dict(jitter=0.5), "fixed step"),
+    (dict(near_mul=2.0), "fixed step"),
+])
+def test_render_proposal_argument_errors(change, msg):
+    net = _net()
+    if "magic" in change:
+        net.magic = change["magic"]
+    ext = capi.LyapRenderExt(proposal=ctypes.pointer(net), proposal_margin=change.get("margin", 0.5),
+                             proposal_segment=change.get("segment", 8), proposal_dilate=change.get("dilate", 0))
+    a, (cam, prm) = _render_args(ext=ctypes.byref(ext))
+    prm.jitter = change.get("jitter", 0.0)
+    prm.nearMultiplier = change.get("near_mul", 1.0)
+    rc = capi.lib.lyap_render(a["cam"], a["prm"], a["seq"], a["seq_len"], a["lights"], a["n_lights"], a["rgba"],
+                              a["points"], a["w"], a["h"], a["ext"], a["stream"])
+    assert rc == capi.LYAP_ERR_INVALID_ARG and msg in capi.last_error(), capi.last_error()
+
+
+def test_render_ext_short_struct_accepted():
+    """A caller built against the struct without the proposal fields passes
+    its own (shorter) size; the size check accepts it (the call then fails
+    later only for want of a device here)."""
+    ext = capi.LyapRenderExt()
+    ext.size = capi.LyapRenderExt.proposal.offset
+    a, keep = _render_args(ext=ctypes.byref(ext))
+    capi.lib.lyap_render(a["cam"], a["prm"], a["seq"], a["seq_len"], a["lights"], a["n_lights"], a["rgba"],
+                         a["points"], a["w"], a["h"], a["ext"], a["stream"])
+    assert "LyapRenderExt.size" not in capi.last_error()
+
+
+def test_net_entry_argument_errors():
+    net = _net()
+    with pytest.raises(capi.LyapError, match="multiple of 128"):
+        capi.net_grad(net, 8, 8, 100, 8)
+    bad = _net()
+    bad.hi[1] = bad.lo[1]
+    with pytest.raises(capi.LyapError, match="empty input box"):
+        capi.net_eval(bad, 8, 4, 8)
+    prm = LyapParams()
+    with pytest.raises(capi.LyapError) as e:
+        capi.net_train(prm, np.array([0, 1, 7, -1], dtype=np.int32))
+    assert e.value.code == capi.LYAP_ERR_SEQUENCE
+    with pytest.raises(capi.LyapError, match="batch"):
+        capi.net_train(prm, np.array([0, 1, -1], dtype=np.int32), batch=100)
