@@ -468,9 +468,58 @@ int lyap_jit_info(char *buf, size_t cap);
 
 /* Measurement support (no reference counterpart): a pipe-rate probe whose
  * launch the caller times.  kind 0 = dependent-chain-free FFMA, kind 1 =
- * lg2.approx; *ops receives the operations performed.  The rate is the
- * denominator of the lambda kernels' FP32 / MUFU roofline. */
+ * lg2.approx, kind 2 = packed FFMA2 (fma.rn.f32x2, two FMAs per lane);
+ * *ops receives the operations performed.  The rate is the denominator of
+ * the lambda kernels' FP32 / MUFU roofline. */
 int lyap_pipe_probe(uint32_t kind, uint32_t iters, float *d_sink, double *ops, void *stream);
+
+/* ---- DOUBLE_REALS render mode ------------------------------------------ */
+/* The reference built with -DDOUBLE_REALS (structs.hpp:10-14, Real =
+ * double): scene_cam_recalculate / scene_lights_recalculate on the double
+ * structs (bit-identical to that build's host code), and kernel_calc_render
+ * with every Real in double on the GPU (lambda's log sum as a renormalised
+ * double product, within ~1e-13 relative of one log per step).  d_counts
+ * (optional, 3 per pixel) receives march / honing / normal samples;
+ * light_model is LYAP_LIGHT_*.  FP64 is this GPU's slow path: the mode is
+ * for precision work.  Asynchronous on stream. */
+int lyap_cam_recalculate_d(LyapCamD *cam, uint32_t tw, uint32_t th, uint32_t td);
+int lyap_lights_recalculate_d(LyapLightD *lights, size_t n);
+int lyap_render_d(const LyapCamD *cam, const LyapParamsD *prm, const int32_t *d_seq, size_t seq_len,
+                  const LyapLightD *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPointD *d_points, uint32_t width,
+                  uint32_t height, uint32_t light_model, uint32_t *d_counts, void *stream);
+
+/* ---- preset, animation path and output files (host only) -------------- */
+/* params_init (params.cu:21-114): the reference's preset parameters, camera
+ * (before scene_cam_recalculate), light(s), sequence string ("BCABA") and
+ * default image size (3840x2160), bit-identical to its host build.  Every
+ * output pointer may be NULL; lights needs light_cap >= 1 (one light is
+ * written, *n_lights = 1).  The _d form is the DOUBLE_REALS build. */
+int lyap_params_init(LyapParams *prm, LyapCam *cam, LyapLight *lights, uint32_t light_cap, uint32_t *n_lights,
+                     char *seq, size_t seq_cap, uint32_t *width, uint32_t *height);
+int lyap_params_init_d(LyapParamsD *prm, LyapCamD *cam, LyapLightD *lights, uint32_t light_cap,
+                       uint32_t *n_lights, char *seq, size_t seq_cap, uint32_t *width, uint32_t *height);
+/* easeInOutQuart of the animation driver (scale.pl:5-11; a quadratic ease). */
+double lyap_ease_in_out_quart(double t, double b, double c, double d);
+/* The camera params.cu's startcalc block computes for interpolation value i
+ * (scale.pl:30-46 substitutes the eased value for params.cu's 1): C and Q
+ * only, other fields untouched.  i is first rounded to 15 significant
+ * digits, as the driver prints it into the source. */
+int lyap_anim_camera(double i, LyapCam *cam);
+int lyap_anim_camera_d(double i, LyapCamD *cam);
+/* save_ppm (lyap_interactive.cu:570-612): "P3\n<w> <h>\n255\n", then
+ * "%3d %3d %3d " per pixel in memory order, then "\n"; binary != 0 writes
+ * P6 instead (an extension).  rgba is host memory. */
+int lyap_write_ppm(const char *path, const RGBA *rgba, uint32_t width, uint32_t height, int binary);
+/* save_points (lyap_interactive.cu:617-652): the LyapPoint array's bytes. */
+int lyap_write_points(const char *path, const LyapPoint *points, size_t n);
+/* lyap_calculate.cu:84-86 (exps.raw): the float volume's bytes, x fastest. */
+int lyap_write_exps(const char *path, const float *values, size_t n);
+/* The reference's output file name (lyap_interactive.cu:576-604):
+ * "<kind>_<stamp>_<w>x<h>_<seq>_cx=.._cy=.._cz=.._step=.._D=.._i=<settle>,
+ * <accum>_d=<depth>_j=.._r=<refine>_ot=.._time=<h>h<mm>m<ss>s.<ext>", kind
+ * "Render" or "Points", cut to 254 characters as the reference's buffers do. */
+int lyap_output_name(char *buf, size_t cap, const char *kind, long stamp, uint32_t width, uint32_t height,
+                     const char *seq, const LyapCam *cam, const LyapParams *prm, uint32_t elapsed_s, const char *ext);
 
 /* ---- learned proposal entry points (no reference counterpart) ----------- */
 /* Trains `net` on the GPU: n_samples + n_val points uniform in the box,

@@ -24,8 +24,12 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "liblyap_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["lyap_render.cu", "lyap_volume.cu", "lyap_capi.cu", "lyap_probe.cu", "lyap_noalloc.cu", "lyap_precise.cu", "lyap_batch.cu", "lyap_net.cu"]
-CXX_SOURCES = ["lyap_scene.cpp", "lyap_jit.cpp"]
+CUDA_SOURCES = ["lyap_render.cu", "lyap_volume.cu", "lyap_capi.cu", "lyap_probe.cu", "lyap_noalloc.cu", "lyap_precise.cu", "lyap_batch.cu", "lyap_net.cu",
+                "lyap_f64.cu"]
+CXX_SOURCES = ["lyap_scene.cpp", "lyap_jit.cpp", "lyap_preset.cpp", "lyap_io.cpp"]
+# the reference front-ends' command-line equivalents (linked against the library)
+CLI_SOURCES = ["lyap_calculate.cpp", "lyap_frame.cpp"]
+CLIDIR = os.path.join(PKG, "cli")
 HEADERS = ["lyap_device.cuh", "lyap_internal.h", "lyap_jobs.h", "lyap_kernels.cuh", "lyap_jit.h", "lyap_net.cuh",
            "lyap_tc.cuh"]
 # headers NVRTC compiles at run time (embedded into the library), and minimal
@@ -63,11 +67,21 @@ def _deps():
             [os.path.join(INCLUDE, "lyap_gb300.h"), os.path.join(INCLUDE, "lyap_kernel.hpp"), __file__])
 
 
+def cli_binary(src):
+    return os.path.join(LIBDIR, os.path.splitext(src)[0])
+
+
 def up_to_date():
     if not os.path.exists(LIB):
         return False
     t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(p) <= t for p in _deps() if os.path.exists(p))
+    if not all(os.path.getmtime(p) <= t for p in _deps() if os.path.exists(p)):
+        return False
+    for c in CLI_SOURCES:
+        b = cli_binary(c)
+        if not os.path.exists(b) or os.path.getmtime(b) < max(t, os.path.getmtime(os.path.join(CLIDIR, c))):
+            return False
+    return True
 
 
 def _run(cmd, verbose):
@@ -130,6 +144,10 @@ def build(force=False, verbose=False, ptxas_verbose=False):
     tmp = LIB + ".tmp"
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs, "-ldl"], verbose)
     os.replace(tmp, LIB)
+    cli_jobs = [[os.environ.get("CXX", "g++"), "-O2", "-std=c++17", f"-I{INCLUDE}", os.path.join(CLIDIR, c), "-o",
+                 cli_binary(c), f"-L{LIBDIR}", "-llyap_gb300", "-Wl,-rpath,$ORIGIN"] for c in CLI_SOURCES]
+    with concurrent.futures.ThreadPoolExecutor(max_workers=len(cli_jobs)) as ex:
+        list(ex.map(lambda c: _run(c, verbose), cli_jobs))
     if ptxas_verbose:
         print("\n".join(l for l in logs if l.strip()))
     return LIB

@@ -142,7 +142,10 @@ EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_
             "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
             "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc", "lyap_jit_info",
             "lyap_lambda_points", "lyap_batch_create", "lyap_batch_run", "lyap_batch_info", "lyap_batch_destroy",
-            "lyap_net_train", "lyap_net_eval", "lyap_net_grad", "lyap_net_save", "lyap_net_load"]
+            "lyap_net_train", "lyap_net_eval", "lyap_net_grad", "lyap_net_save", "lyap_net_load",
+            "lyap_params_init", "lyap_params_init_d", "lyap_ease_in_out_quart", "lyap_anim_camera",
+            "lyap_anim_camera_d", "lyap_write_ppm", "lyap_write_points", "lyap_write_exps", "lyap_output_name",
+            "lyap_cam_recalculate_d", "lyap_lights_recalculate_d", "lyap_render_d"]
 
 
 def _load():
@@ -181,9 +184,25 @@ def _load():
     L.lyap_net_grad.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
     L.lyap_net_save.argtypes = [c_void_p, c_char_p]
     L.lyap_net_load.argtypes = [c_void_p, c_char_p]
+    L.lyap_params_init.argtypes = [c_void_p, c_void_p, c_void_p, c_uint32, POINTER(c_uint32), c_char_p, c_size_t,
+                                   POINTER(c_uint32), POINTER(c_uint32)]
+    L.lyap_params_init_d.argtypes = L.lyap_params_init.argtypes
+    L.lyap_ease_in_out_quart.argtypes = [ctypes.c_double] * 4
+    L.lyap_cam_recalculate_d.argtypes = [c_void_p, c_uint32, c_uint32, c_uint32]
+    L.lyap_lights_recalculate_d.argtypes = [c_void_p, c_size_t]
+    L.lyap_render_d.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_uint32, c_void_p, c_void_p,
+                                c_uint32, c_uint32, c_uint32, c_void_p, c_void_p]
+    L.lyap_anim_camera.argtypes = [ctypes.c_double, c_void_p]
+    L.lyap_anim_camera_d.argtypes = [ctypes.c_double, c_void_p]
+    L.lyap_write_ppm.argtypes = [c_char_p, c_void_p, c_uint32, c_uint32, c_int]
+    L.lyap_write_points.argtypes = [c_char_p, c_void_p, c_size_t]
+    L.lyap_write_exps.argtypes = [c_char_p, c_void_p, c_size_t]
+    L.lyap_output_name.argtypes = [c_char_p, c_size_t, c_char_p, ctypes.c_long, c_uint32, c_uint32, c_char_p,
+                                   c_void_p, c_void_p, c_uint32, c_char_p]
     for name in EXPORTED:
         if name not in ("lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_status_string"):
             getattr(L, name).restype = c_int
+    L.lyap_ease_in_out_quart.restype = ctypes.c_double
     return L
 
 
@@ -421,3 +440,78 @@ def net_from_params(params, lo, hi):
     assert p.size == NET_PARAMS
     ctypes.memmove(net.params, p.ctypes.data, p.nbytes)
     return net
+
+
+# ---- preset, animation path and output files --------------------------------
+def params_init(double=False):
+    """lyap_params_init(_d): (params, camera, lights, sequence string, (width, height))."""
+    from .types import LyapCamD, LyapLightD, LyapParamsD
+    prm, cam = (LyapParamsD(), LyapCamD()) if double else (LyapParams(), LyapCam())
+    lights = ((LyapLightD if double else LyapLight) * 4)()
+    n = c_uint32(0)
+    seq = ctypes.create_string_buffer(64)
+    w, h = c_uint32(0), c_uint32(0)
+    fn = lib.lyap_params_init_d if double else lib.lyap_params_init
+    _check(fn(ctypes.byref(prm), ctypes.byref(cam), lights, 4, ctypes.byref(n), seq, 64, ctypes.byref(w),
+              ctypes.byref(h)))
+    return prm, cam, list(lights)[:n.value], seq.value.decode(), (w.value, h.value)
+
+
+def ease_in_out_quart(t, b=0.0, c=1.0, d=1.0):
+    return lib.lyap_ease_in_out_quart(t, b, c, d)
+
+
+def anim_camera(i, cam=None, double=False):
+    """The camera of the animation path at eased value i (C and Q set on a copy of cam)."""
+    from .types import LyapCamD
+    if cam is None:
+        cam = params_init(double)[1]
+    c = (LyapCamD if double else LyapCam).from_buffer_copy(cam)
+    _check((lib.lyap_anim_camera_d if double else lib.lyap_anim_camera)(i, ctypes.byref(c)))
+    return c
+
+
+def write_ppm(path, rgba, binary=False):
+    a = np.ascontiguousarray(rgba, dtype=np.uint8)
+    h, w = a.shape[:2]
+    _check(lib.lyap_write_ppm(os.fsencode(path), _vp(a), w, h, 1 if binary else 0))
+
+
+def write_points(path, points):
+    a = np.ascontiguousarray(points)
+    _check(lib.lyap_write_points(os.fsencode(path), _vp(a), a.size))
+
+
+def write_exps(path, values):
+    a = np.ascontiguousarray(values, dtype=np.float32)
+    _check(lib.lyap_write_exps(os.fsencode(path), _vp(a), a.size))
+
+
+def output_name(kind, stamp, width, height, seq, cam, prm, elapsed_s, ext):
+    buf = ctypes.create_string_buffer(512)
+    _check(lib.lyap_output_name(buf, 512, kind.encode(), stamp, width, height, seq.encode(), ctypes.byref(cam),
+                                ctypes.byref(prm), elapsed_s, ext.encode()))
+    return buf.value.decode()
+
+
+# ---- DOUBLE_REALS render mode ---------------------------------------------
+def cam_recalculate_d(cam, tw, th, td=1):
+    from .types import LyapCamD
+    c = LyapCamD.from_buffer_copy(cam)
+    _check(lib.lyap_cam_recalculate_d(ctypes.byref(c), tw, th, td))
+    return c
+
+
+def lights_recalculate_d(lights):
+    from .types import LyapLightD
+    arr = (LyapLightD * max(1, len(lights)))(*[LyapLightD.from_buffer_copy(l) for l in lights])
+    _check(lib.lyap_lights_recalculate_d(arr, len(lights)))
+    return list(arr)[:len(lights)]
+
+
+def render_d(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height,
+             light_model=LIGHT_SPOT, d_counts=None, stream=None):
+    """lyap_render_d: the DOUBLE_REALS render on device buffers (points: 72 bytes each)."""
+    _check(lib.lyap_render_d(ctypes.byref(cam), ctypes.byref(prm), _vp(d_seq), seq_len, _vp(d_lights), n_lights,
+                             _vp(d_rgba), _vp(d_points), width, height, light_model, _vp(d_counts),
+                             _stream(stream)))

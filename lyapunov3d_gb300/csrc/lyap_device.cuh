@@ -499,11 +499,12 @@ __device__ __forceinline__ double pick_d(uint32_t sym, double x, double y, doubl
     return (sym & 2u) ? hi : lo;
 }
 
-static __device__ __noinline__ double lambda_f64(double x, double y, double z, const SeqInfo &si)
+static __device__ __noinline__ double lambda_f64_core(double x, double y, double z, double d, const int32_t *seq,
+                                                      uint32_t L, uint32_t S, uint32_t A)
 {
-    const double d = (double)si.d;
-    const int32_t *seq = si.seq;
-    const uint32_t L = si.L;
+    struct {
+        uint32_t S, A;
+    } si = {S, A};
     double v = 0.5;
     uint32_t k = 0;
     for (uint32_t n = 0; n < si.S; n++) {
@@ -551,6 +552,12 @@ static __device__ __noinline__ double lambda_f64(double x, double y, double z, c
         l = ((double)e + log2(p)) * 0.693147180559945309417232121458176568;
     }
     return l / (double)si.A;
+}
+
+// lambda in double at a float parameter d (the float-params callers)
+static __device__ __forceinline__ double lambda_f64(double x, double y, double z, const SeqInfo &si)
+{
+    return lambda_f64_core(x, y, z, (double)si.d, si.seq, si.L, si.S, si.A);
 }
 
 // --------------------------------------------------------------- the ray

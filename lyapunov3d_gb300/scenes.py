@@ -168,7 +168,7 @@ def small_volume(n=64):
     return VolumeWorkload(f"volume{n}_abc_20+100", (n, n, n), (2.5, 2.5, 2.5), (4.0, 4.0, 4.0), "ABC", prm)
 
 
-def full_render(seed=1, width=1920, height=1080):
+def full_render(seed=1, width=1920, height=1080, seq=None):
     """1920x1080, 512 uniform steps per ray (method 1, no jitter), seeded
     12-symbol sequence over {A, B, C}, 200 + 1000 iterations over [2, 4]^3,
     camera uniform on S^3 at distance 5-8 from the cube centre, one
@@ -178,7 +178,8 @@ def full_render(seed=1, width=1920, height=1080):
     ray crosses the weakly stable shell before it stops, ~140 samples per
     ray inside the box for seed 1."""
     rng = SplitMix64(0x4C594150_00000000 | seed)
-    seq = random_sequence(rng, 12)
+    drawn = random_sequence(rng, 12)
+    seq = drawn if seq is None else seq   # a given sequence replaces the drawn one; the camera stays
     q = uniform_quaternion(rng)
     dist = rng.uniform(5.0, 8.0)
     cam = orbit_camera(q, (3.0, 3.0, 3.0), dist)
@@ -187,7 +188,8 @@ def full_render(seed=1, width=1920, height=1080):
     light = headlight(cam, ambient=(0.08, 0.08, 0.08, 1.0))
     lq = uniform_quaternion(rng)
     light.Q.x, light.Q.y, light.Q.z, light.Q.w = lq
-    return RenderWorkload(f"frame1080_seq12_200+1000_seed{seed}", width, height, seq, prm, cam,
+    tag = "seq12" if seq == drawn else f"seq{seq}"
+    return RenderWorkload(f"frame{height}_{tag}_200+1000_seed{seed}", width, height, seq, prm, cam,
                           [light], light_model=1)
 
 

@@ -140,6 +140,15 @@ class Oracle:
         rc = self.lib.orc_raymarch(mode, ctypes.byref(pt), sx, sy, ctypes.byref(cam), ctypes.byref(prm), _ptr(s), cnt)
         return rc, pt, tuple(cnt)
 
+    def raymarch_d(self, sx, sy, cam, prm, seq):
+        """orc_raymarch_d: the DOUBLE_REALS raymarch of one pixel."""
+        s = _seq_array(seq)
+        pt = LyapPointD()
+        ctypes.memset(ctypes.byref(pt), 0xFF, ctypes.sizeof(pt))
+        cnt = (c_uint32 * 3)()
+        rc = self.lib.orc_raymarch_d(ctypes.byref(pt), sx, sy, ctypes.byref(cam), ctypes.byref(prm), _ptr(s), cnt)
+        return rc, pt, tuple(cnt)
+
     def shade(self, pt, cam, lights):
         arr = (LyapLight * max(1, len(lights)))(*[LyapLight.from_buffer_copy(l) for l in lights])
         col = (c_float * 4)()
