@@ -55,7 +55,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
     ap.add_argument("--volume", type=int, default=512, help="edge of the secondary volume sweep (0 = skip)")
     ap.add_argument("--no-jit", action="store_true", help="precompiled kernels only (no run-time specialisation)")
-    ap.add_argument("--report", choices=["precision", "batch"], default=None,
+    ap.add_argument("--margins", default="0.25,0.5,0.75,1.0,1.25",
+                    help="--report proposal: skip thresholds above the opaque threshold")
+    ap.add_argument("--proposal-segment", type=int, default=8, help="--report proposal: samples per segment")
+    ap.add_argument("--train-steps", type=int, default=8192, help="--report proposal: Adam steps")
+    ap.add_argument("--report", choices=["precision", "batch", "proposal"], default=None,
                     help="instead of the benchmark, print the precision form's error report or time the batch")
     ap.add_argument("--batch-scale", type=int, default=1, help="--report batch: divide every image side by this")
     return ap.parse_args()
@@ -417,16 +421,16 @@ def run_ours(args):
 
 def run_precision_report(args):
     """The precision form on the CPU-runnable workload (ABC, 20 + 100, [2.5, 4]^3):
-    lambda of the plain, product and FP64 forms at 2^20 seeded points against
-    the FP64 oracle; a 128^2 frame rendered with the product form and FP64
-    bisection (20 halvings) of every crossing, its hit-point lambdas against
-    the oracle, and its surface agreement with the plain frame."""
+    lambda of the plain and product forms at 2^20 seeded points against the
+    FP64 form (lambda in double on the GPU, which tests/test_gpu_precision.py
+    holds to the FP64 oracle within 1e-14); a 128^2 frame rendered with the
+    product form and FP64 bisection (20 halvings) of every crossing, its
+    hit-point lambdas against the FP64 form, and its surface agreement with
+    the plain frame."""
     import torch
     from lyapunov3d_gb300 import capi, scenes
     from lyapunov3d_gb300.device import DeviceFrame
-    from oracle import ORC_F64, Oracle
     dev = torch.device("cuda", 0)
-    orc = Oracle()
     wl = scenes.small_render(128)
     prm = wl.params
     seq = capi.seq_parse(wl.seq)
@@ -434,10 +438,9 @@ def run_precision_report(args):
     n = 1 << 20
     pts = np.random.default_rng(20240).uniform(prm.lMin, prm.lMax, size=(n, 3)).astype(np.float32)
     d_xyz = torch.from_numpy(pts.reshape(-1)).to(dev)
-    pts4 = np.column_stack([pts.astype(np.float64), np.full(n, prm.d)])
-    t0 = time.perf_counter()
-    ref = orc.lyap4d(ORC_F64, pts4, prm.settle, prm.accum, seq)
-    t_orc = time.perf_counter() - t0
+    o64 = torch.empty(n, dtype=torch.float64, device=dev)
+    capi.lambda_points(d_xyz, n, prm, d_seq, seq.size, capi.FORM_F64, o64)
+    ref = o64.cpu().numpy()
     fin = np.isfinite(ref)
 
     def stats(got):
@@ -448,12 +451,9 @@ def run_precision_report(args):
                 "p99_abs": float(np.quantile(d, 0.99)), "nan_mismatch": int((np.isnan(g) != np.isnan(ref)).sum())}
     out = {}
     o32 = torch.empty(n, dtype=torch.float32, device=dev)
-    o64 = torch.empty(n, dtype=torch.float64, device=dev)
     for name, form in [("plain", capi.VARIANT_PLAIN), ("product", capi.VARIANT_PRODUCT)]:
         capi.lambda_points(d_xyz, n, prm, d_seq, seq.size, form, o32)
         out[name] = stats(o32.cpu().numpy())
-    capi.lambda_points(d_xyz, n, prm, d_seq, seq.size, capi.FORM_F64, o64)
-    out["f64_gpu"] = stats(o64.cpu().numpy())
 
     f = DeviceFrame(wl, device=dev, counts=True)
     f.run(capi.VARIANT_PLAIN)
@@ -463,19 +463,20 @@ def run_precision_report(args):
     torch.cuda.synchronize()
     pp = f.points()
     hit, phit = ~np.isnan(pp["a"]), ~np.isnan(plain_pts["a"])
-    P = pp["P"][hit].astype(np.float32)
-    href = orc.lyap4d(ORC_F64, np.column_stack([P.astype(np.float64), np.full(len(P), prm.d)]), prm.settle,
-                      prm.accum, seq)
-    d_P = torch.from_numpy(np.ascontiguousarray(P).reshape(-1)).to(dev)
+    P = np.ascontiguousarray(pp["P"][hit].astype(np.float32))
+    d_P = torch.from_numpy(P.reshape(-1)).to(dev)
+    h64 = torch.empty(len(P), dtype=torch.float64, device=dev)
     hp = torch.empty(len(P), dtype=torch.float32, device=dev)
+    capi.lambda_points(d_P, len(P), prm, d_seq, seq.size, capi.FORM_F64, h64)
     capi.lambda_points(d_P, len(P), prm, d_seq, seq.size, capi.VARIANT_PRODUCT, hp)
+    href = h64.cpu().numpy()
     hp = hp.cpu().numpy().astype(np.float64)
     ok = np.isfinite(href) & np.isfinite(hp)
     stored = pp["l"][hit].astype(np.float64)
     ok2 = np.isfinite(href) & np.isfinite(stored)
     report = {
-        "workload": wl.name, "points": n, "oracle_seconds": t_orc, "oracle_threads": orc.threads(),
-        "lambda_vs_f64_oracle_at_points": out,
+        "workload": wl.name, "points": n, "reference": "FP64 form on the GPU (lyap_lambda_points, LYAP_FORM_F64)",
+        "lambda_vs_f64_at_points": out,
         "frame": {"pixels": int(hit.size), "hits": int(hit.sum()), "plain_hits": int(phit.sum()),
                   "surface_pixel_agreement_vs_plain": float((hit == phit).mean()),
                   "hit_lambda_product_vs_f64": {"max_abs": float(np.abs(hp[ok] - href[ok]).max()),
@@ -522,8 +523,77 @@ def run_batch_report(args):
         "chunks": info.chunks}), flush=True)
 
 
+def run_proposal_report(args):
+    """The learned proposal on the 1080p frame (scenes.full_render): the net
+    trained on the GPU (2^20 plain-method lambda samples; its kernels'
+    gradients are checked against the CPU oracle in tests/test_gpu_net.py),
+    then the product-form frame with
+    the proposal at each margin against the same frame without it (and with
+    an untrained net at the same margins): device time, lambda samples
+    evaluated, surface agreement (pixels hit in both / hit by the plain
+    march) and same-sample agreement (hit at the bit-identical point)."""
+    import ctypes
+    import torch
+    from lyapunov3d_gb300 import capi, scenes
+    from lyapunov3d_gb300.device import DeviceFrame
+    dev = torch.device("cuda", 0)
+    wl = scenes.full_render(args.seed, args.width, args.height)
+    seq = capi.seq_parse(wl.seq)
+    t0 = time.perf_counter()
+    net, loss = capi.net_train(wl.params, seq, steps=args.train_steps, seed=args.seed, with_loss=True)
+    t_train = time.perf_counter() - t0
+    untrained = capi.net_train(wl.params, seq, steps=1, seed=args.seed)
+    frame = DeviceFrame(wl, device=dev, counts=False)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(128 << 20, dtype=torch.float32, device=dev)
+
+    def timed(**kw):
+        for _ in range(max(1, args.warmup)):
+            frame.run(capi.VARIANT_PRODUCT, stream=stream, jit=True, **kw)
+        torch.cuda.synchronize()
+        frame.reset_stats()
+        ts = []
+        for i in range(max(1, args.steps)):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            frame.run(capi.VARIANT_PRODUCT, stream=stream, jit=True, **kw)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts), frame.stats() // max(1, args.steps), frame.d_points.view(-1, 9).cpu().numpy()
+
+    ms0, st0, p0 = timed()
+    hit0 = ~np.isnan(p0[:, 0])
+    rows = []
+    for which, n in (("trained", net), ("untrained", untrained)):
+        for m in (float(x) for x in args.margins.split(",")):
+            ms, st, p1 = timed(proposal=ctypes.pointer(n), proposal_margin=m, proposal_segment=args.proposal_segment)
+            hit1 = ~np.isnan(p1[:, 0])
+            same = hit0 & hit1 & (p0[:, :3].view(np.uint32) == p1[:, :3].view(np.uint32)).all(1)
+            rows.append({"net": which, "margin": m, "ms": ms, "speedup": ms0 / ms,
+                         "samples_evaluated_frac": float(st[capi.STAT_SAMPLES] / st0[capi.STAT_SAMPLES]),
+                         "samples_skipped": int(st[capi.STAT_PROPOSAL_SKIPPED]),
+                         "net_points": int(st[capi.STAT_PROPOSAL_POINTS]),
+                         "net_timeouts": int(st[capi.STAT_NET_TIMEOUTS]),
+                         "surface_agreement": float(hit1.sum() / max(1, hit0.sum())),
+                         "same_sample_agreement": float(same.sum() / max(1, hit0.sum())),
+                         "extra_hits": int((hit1 & ~hit0).sum())})
+    print(json.dumps({
+        "report": "proposal", "workload": wl.name, "width": wl.width, "height": wl.height,
+        "train": {"seconds": t_train, "steps": net.steps, "batch": net.batch, "samples": net.n_samples,
+                  "train_mse": net.train_mse, "val_mse": net.val_mse,
+                  "loss_first10": float(np.mean(loss[:10])), "loss_last100": float(np.mean(loss[-100:]))},
+        "segment": args.proposal_segment,
+        "without_proposal": {"ms": ms0, "samples": int(st0[capi.STAT_SAMPLES]), "hits": int(hit0.sum())},
+        "with_proposal": rows}), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.report == "proposal":
+        run_proposal_report(args)
+        return
     if args.report == "precision":
         run_precision_report(args)
         return
