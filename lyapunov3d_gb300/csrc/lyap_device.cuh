@@ -345,6 +345,38 @@ struct UnrollC {
     static constexpr bool aligned8 = (U % 8) == 0;   // renormalisation points fall on j % 8 == 7
 };
 
+// ---------------------------------------------------- packed FP32 pairs
+// fma.rn.f32x2 / mul.rn.f32x2 round each half exactly as fma.rn.f32 /
+// mul.rn.f32 do; one instruction carries two samples' operations, which
+// halves the issue slots of the FP32 work (the FP32 pipe rate is unchanged).
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi)
+{
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b)
+{
+    uint64_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c)
+{
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+template <class SS, class SA>
+__device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const float (&py)[2], const float (&pz)[2],
+                                                float d, uint32_t S, uint32_t A, float (&out)[2],
+                                                uint32_t &skipped, uint32_t &fallback);
+
 // K samples (px[k], py[k], pz[k]) with the settle symbols SS and the
 // accumulation symbols SA (SS rotated by settle mod L).  Same arithmetic as
 // lambda_fixed, sample by sample.  skipped / fallback: bit k set for sample k.
@@ -353,6 +385,10 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
                                              float d, uint32_t S, uint32_t A, float (&out)[K],
                                              uint32_t &skipped, uint32_t &fallback)
 {
+    if constexpr (MODE == MODE_PRODUCT && K == 2) {
+        lambda_const_x2<SS, SA>(px, py, pz, d, S, A, out, skipped, fallback);
+        return;
+    }
     constexpr int L = SS::L;
     constexpr int U = UnrollC<L>::U;
     static_assert(UnrollC<L>::aligned8 || MODE == MODE_PLAIN, "product form needs U % 8 == 0");
@@ -471,6 +507,112 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
         // an intermediate product may have been subnormal: redo those samples in the plain form
 #pragma unroll
         for (int k = 0; k < K; k++) {
+            if ((fallback >> k) & 1u) {
+                const float qx[1] = {px[k]}, qy[1] = {py[k]}, qz[1] = {pz[k]};
+                float o[1];
+                uint32_t sk, fb;
+                lambda_const<MODE_PLAIN, 1, SS, SA>(qx, qy, qz, d, S, A, o, sk, fb);
+                out[k] = o[0];
+            }
+        }
+    }
+}
+
+// The product form for two samples at once on packed FP32 pairs.  The
+// state is kept negated, s = -v, so that every operation is a plain packed
+// mul / fma with the scalar form's rounding:
+//   mt = r*s        = -(r*v)                   (the scalar t, negated)
+//   s' = mt*s + mt  = -(t - t*v)               (the scalar fma(-t, v, t), negated)
+//   d  = (2r)*s' + r = r - 2r*v'               (the scalar fma(-2r, v', r))
+//   p' = p*d                                    (|p'| = the scalar p*|d|)
+// Round-to-nearest is symmetric, so each quantity is the scalar one or its
+// exact negation; renorm discards the sign of p.
+template <class SS, class SA>
+__device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const float (&py)[2], const float (&pz)[2],
+                                                float d, uint32_t S, uint32_t A, float (&out)[2],
+                                                uint32_t &skipped, uint32_t &fallback)
+{
+    constexpr int L = SS::L;
+    constexpr int U = UnrollC<L>::U;
+    static_assert(UnrollC<L>::aligned8, "product form needs U % 8 == 0");
+    const uint64_t R[4] = {f2_pack(px[0], px[1]), f2_pack(py[0], py[1]), f2_pack(pz[0], pz[1]), f2_pack(d, d)};
+    const uint64_t TR[4] = {f2_pack(2.0f * px[0], 2.0f * px[1]), f2_pack(2.0f * py[0], 2.0f * py[1]),
+                            f2_pack(2.0f * pz[0], 2.0f * pz[1]), f2_pack(2.0f * d, 2.0f * d)};
+    uint64_t s = f2_pack(-0.5f, -0.5f);
+    {
+        const uint32_t nb = S / U, rem = S - nb * U;
+        for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+            for (int j = 0; j < U; j++) {
+                const uint64_t mt = f2_mul(R[SS::at(j % L)], s);
+                s = f2_fma(mt, s, mt);
+            }
+        }
+        uint32_t jj = 0;
+        for (uint32_t j = 0; j < rem; j++) {
+            const uint32_t sym = SS::at_rt(jj);
+            jj = (jj + 1 == (uint32_t)L) ? 0 : jj + 1;
+            const uint64_t r = (sym & 2u) ? ((sym & 1u) ? R[3] : R[2]) : ((sym & 1u) ? R[1] : R[0]);
+            const uint64_t mt = f2_mul(r, s);
+            s = f2_fma(mt, s, mt);
+        }
+    }
+    skipped = 0;
+    fallback = 0;
+    {
+        float s0, s1;
+        f2_unpack(s, s0, s1);
+        const float v0 = -s0, v1 = -s1;
+        if (!(v0 < 0.5f || v0 > 0.5f)) skipped |= 1u;
+        if (!(v1 < 0.5f || v1 > 0.5f)) skipped |= 2u;
+    }
+    uint64_t p = f2_pack(1.0f, 1.0f);
+    int32_t e0 = 0, e1 = 0;
+    uint32_t bad0 = 0, bad1 = 0;
+    auto renorm2 = [&]() {
+        float a, b;
+        f2_unpack(p, a, b);
+        renorm(a, e0, bad0);
+        renorm(b, e1, bad1);
+        p = f2_pack(a, b);
+    };
+    const uint32_t nb = A / U, rem = A - nb * U;
+    for (uint32_t b = 0; b < nb; b++) {
+#pragma unroll
+        for (int j = 0; j < U; j++) {
+            const uint32_t sym = SA::at(j % L);
+            const uint64_t mt = f2_mul(R[sym], s);
+            s = f2_fma(mt, s, mt);
+            p = f2_mul(p, f2_fma(TR[sym], s, R[sym]));
+            if ((j & 7) == 7) renorm2();
+        }
+    }
+    uint32_t jj = 0;
+    for (uint32_t j = 0; j < rem; j++) {
+        const uint32_t sym = SA::at_rt(jj);
+        jj = (jj + 1 == (uint32_t)L) ? 0 : jj + 1;
+        const uint64_t r = (sym & 2u) ? ((sym & 1u) ? R[3] : R[2]) : ((sym & 1u) ? R[1] : R[0]);
+        const uint64_t tr = (sym & 2u) ? ((sym & 1u) ? TR[3] : TR[2]) : ((sym & 1u) ? TR[1] : TR[0]);
+        const uint64_t mt = f2_mul(r, s);
+        s = f2_fma(mt, s, mt);
+        p = f2_mul(p, f2_fma(tr, s, r));
+        if ((j & 7u) == 7u) renorm2();
+    }
+    renorm2();
+    float p0, p1;
+    f2_unpack(p, p0, p1);
+    const int32_t bias = (int32_t)(127u * (A / 8 + 1));
+    float l2[2] = {(float)(e0 - bias) + lg2_approx(p0), (float)(e1 - bias) + lg2_approx(p1)};
+    if (bad0 && !(skipped & 1u)) fallback |= 1u;
+    if (bad1 && !(skipped & 2u)) fallback |= 2u;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const float lk = ((skipped >> k) & 1u) ? 0.0f : l2[k];
+        out[k] = f_isfinite(lk) ? (lk * LN2F) / (float)A : __int_as_float(0x7fffffff);
+    }
+    if (fallback) {
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
             if ((fallback >> k) & 1u) {
                 const float qx[1] = {px[k]}, qy[1] = {py[k]}, qz[1] = {pz[k]};
                 float o[1];

@@ -112,6 +112,15 @@ bool jit_disabled_by_env()
 
 // Resident render blocks per SM the specialised kernel is compiled for
 // (its register cap); LYAP_JIT_RENDER_BLOCKS=4..8 overrides the default.
+// paired rounds in the specialised render (LYAP_RENDER_PAIRS): environment
+// LYAP_JIT_PAIRS=0/1 overrides the default
+int jit_render_pairs()
+{
+    const char *v = getenv("LYAP_JIT_PAIRS");
+    if (v && (v[0] == '0' || v[0] == '1')) return v[0] - '0';
+    return LYAP_JIT_RENDER_PAIRS;
+}
+
 int jit_render_min_blocks()
 {
     const char *v = getenv("LYAP_JIT_RENDER_BLOCKS");
@@ -119,7 +128,8 @@ int jit_render_min_blocks()
         const int n = atoi(v);
         if (n >= 2 && n <= 16) return n;
     }
-    return LYAP_JIT_RENDER_MIN_BLOCKS;
+    // two samples per lane need ~96 registers: 5 blocks of 128 threads per SM
+    return jit_render_pairs() ? LYAP_JIT_RENDER_MIN_BLOCKS - 1 : LYAP_JIT_RENDER_MIN_BLOCKS;
 }
 
 std::string hex64(uint64_t v)
@@ -181,8 +191,9 @@ void compile_entry(Entry &e, const Spec &s)
     for (auto &n : names) N.add_name(prog, n.c_str());
     const std::string rmin = "-DLYAP_RENDER_MIN_BLOCKS=" + std::to_string(jit_render_min_blocks());
     const std::string vmin = "-DLYAP_VOLUME_MIN_BLOCKS=" + std::to_string(LYAP_JIT_VOLUME_MIN_BLOCKS);
+    const std::string pairs = "-DLYAP_RENDER_PAIRS=" + std::to_string(jit_render_pairs());
     const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-fmad=false", "-lineinfo",
-                          "--ptxas-options=-v", rmin.c_str(), vmin.c_str()};
+                          "--ptxas-options=-v", rmin.c_str(), vmin.c_str(), pairs.c_str()};
     r = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
     size_t ls = 0;
     N.log_size(prog, &ls);

@@ -14,6 +14,8 @@
 // 256 threads per SM).
 #define LYAP_JIT_MAX_PERIOD 32
 #define LYAP_JIT_RENDER_MIN_BLOCKS 6
+// paired rounds (two samples per lane, packed FP32 pairs) in the specialised render
+#define LYAP_JIT_RENDER_PAIRS 0
 #define LYAP_RENDER_THREADS_JIT 128
 #define LYAP_JIT_VOLUME_K 2
 #define LYAP_JIT_VOLUME_MIN_BLOCKS 4

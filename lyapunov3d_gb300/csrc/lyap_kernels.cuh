@@ -28,6 +28,9 @@
 #ifndef LYAP_RENDER_MIN_BLOCKS
 #define LYAP_RENDER_MIN_BLOCKS 4
 #endif
+#ifndef LYAP_RENDER_PAIRS
+#define LYAP_RENDER_PAIRS 0
+#endif
 #ifndef LYAP_VOLUME_THREADS
 #define LYAP_VOLUME_THREADS 256
 #endif
@@ -311,6 +314,133 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     return res;
 }
 
+// Paired rounds (LYAP_RENDER_PAIRS): every lane evaluates two lambda samples
+// per round as one packed evaluation (Lam::eval<2>; the product form runs both
+// on FP32 pairs, fma.rn.f32x2).  Slot 0 is what sample_round evaluates; slot 1
+// is the same ray's next sample when its position is already known -- the
+// next march step when the step length is fixed and no proposal is active, or
+// the next normal sample -- else a dummy.  Lanes without a ray take the next
+// samples of running rays two at a time: helper (owner, j) evaluates the
+// owner's samples 2j and 2j+1 ahead.  The rays consume the results in order,
+// exactly as sample_round does one by one.
+__device__ __forceinline__ V3 sample_ahead(V3 P, V3 V, float dt, float mag, uint32_t phase, uint32_t offset,
+                                           bool &valid)
+{
+    if (phase <= PH_MARCH) {
+        for (uint32_t j = 0; j < offset; j++) P = P + V * dt;   // as ray_advance adds the steps
+        valid = true;
+        return P;
+    }
+    const uint32_t k = phase - PH_NORM0 + offset;
+    valid = k <= 5u;
+    Ray tmp;
+    tmp.P = P;
+    tmp.mag = mag;
+    tmp.phase = PH_NORM0 + (k > 5u ? 5u : k);
+    return ray_sample_point(tmp);
+}
+
+template <class Lam>
+__device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, const uint32_t amask, const Lam &lam,
+                                                 const LyapParams &prm, const bool fixed_step, const bool spec_ok,
+                                                 const bool bracket_mode, LaneStats &st)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    // can this ray's next positions be known before its current sample's lambda?
+    const bool ahead = active && ((fixed_step && r.phase <= PH_MARCH) ||
+                                  (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5));
+    uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
+    bool helper = false;
+    uint32_t owner = lane, offset = 0;
+    if (spec_ok && amask != FULL) {
+        emask = __ballot_sync(FULL, ahead);
+        ne = __popc(emask);
+        if (ne) {
+            imask = ~amask;
+            ni = __popc(imask);
+            maxj = (ni + ne - 1) / ne;
+            if (!active) {
+                const uint32_t rank = __popc(imask & ((1u << lane) - 1u));
+                owner = nth_set_bit(emask, rank % ne);
+                offset = 2 + 2 * (rank / ne);
+                helper = true;
+            }
+        }
+    }
+    V3 Q0 = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
+    V3 Q1 = v3(3.0f, 3.0f, 3.0f);
+    if (ahead) {
+        bool v;
+        Q1 = sample_ahead(r.P, r.V, r.dt, r.mag, r.phase, 1u, v);
+    }
+    if (ne) {
+        V3 oP, oV;
+        oP.x = __shfl_sync(FULL, r.P.x, owner);
+        oP.y = __shfl_sync(FULL, r.P.y, owner);
+        oP.z = __shfl_sync(FULL, r.P.z, owner);
+        oV.x = __shfl_sync(FULL, r.V.x, owner);
+        oV.y = __shfl_sync(FULL, r.V.y, owner);
+        oV.z = __shfl_sync(FULL, r.V.z, owner);
+        const float odt = __shfl_sync(FULL, r.dt, owner);
+        const float omag = __shfl_sync(FULL, r.mag, owner);
+        const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
+        if (helper) {
+            bool v0, v1;
+            Q0 = sample_ahead(oP, oV, odt, omag, ophase, offset, v0);
+            Q1 = sample_ahead(oP, oV, odt, omag, ophase, offset + 1u, v1);
+            st.spec += (v0 ? 1u : 0u) + (v1 ? 1u : 0u);
+        }
+    }
+
+    st.rounds += 1;
+    st.lane_rounds += __popc(amask) + (ne ? (ni < maxj * ne ? ni : maxj * ne) : 0u);
+    const float qx[2] = {Q0.x, Q1.x}, qy[2] = {Q0.y, Q1.y}, qz[2] = {Q0.z, Q1.z};
+    float lv[2];
+    uint32_t skb, fbb;
+    lam.template eval<2>(qx, qy, qz, lv, skb, fbb);
+    int res = RAY_CONTINUE;
+    uint32_t kind = 0;   // 1: march, 2: normal
+    if (active) {
+        kind = (r.phase <= PH_MARCH) ? 1u : (r.phase >= PH_NORM0 ? 2u : 0u);
+        st.samples += 1;
+        st.skipped += skb & 1u;
+        st.fallback += fbb & 1u;
+        res = ray_advance(r, lv[0], prm, bracket_mode);
+        const bool same = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
+        if (ahead && res == RAY_CONTINUE && same) {
+            st.samples += 1;
+            st.skipped += (skb >> 1) & 1u;
+            st.fallback += (fbb >> 1) & 1u;
+            res = ray_advance(r, lv[1], prm, bracket_mode);
+        }
+    }
+    if (ne) {
+        const bool own_elig = (emask >> lane) & 1u;
+        const uint32_t idx = __popc(emask & ((1u << lane) - 1u));
+        const uint32_t bits = skb | (fbb << 2);
+        for (uint32_t j = 1; j <= maxj; j++) {
+            const uint32_t rr = (j - 1) * ne + idx;
+            const bool have = own_elig && rr < ni;
+            const uint32_t src = have ? nth_set_bit(imask, rr) : lane;
+            const float l0 = __shfl_sync(FULL, lv[0], src);
+            const float l1 = __shfl_sync(FULL, lv[1], src);
+            const uint32_t b = __shfl_sync(FULL, bits, src);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const bool same = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
+                if (have && res == RAY_CONTINUE && same) {
+                    st.samples += 1;
+                    st.skipped += (b >> h) & 1u;
+                    st.fallback += (b >> (2 + h)) & 1u;
+                    st.spec_used += 1;
+                    res = ray_advance(r, h ? l1 : l0, prm, bracket_mode);
+                }
+            }
+        }
+    }
+    return res;
+}
+
 // Learned proposal: at the start of every march segment the net marked empty
 // the ray takes the segment's steps without evaluating lambda.  Each step is
 // the one ray_advance takes after a sample above the opaque threshold (count
@@ -360,8 +490,8 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
     const CamRays cr = cam_rays(job.cam);
     // march positions are known ahead only with a fixed step length
     // (with a proposal the march positions depend on its skips: no speculation)
-    const bool spec_ok = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f) &&
-                         !(job.flags & LYAP_FLAG_NO_SPECULATION) && job.skip == nullptr;
+    const bool fixed_step = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f) && job.skip == nullptr;
+    const bool spec_ok = fixed_step && !(job.flags & LYAP_FLAG_NO_SPECULATION);
     const bool bracket_mode = (job.flags & LYAP_FLAG_BISECT_F64) != 0u;
     LaneStats st = {};
     Ray r;
@@ -404,7 +534,11 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
         const uint32_t amask = __ballot_sync(FULL, active);
         if (amask == 0) break;
 
+#if LYAP_RENDER_PAIRS
+        int res = sample_round_pair(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, st);
+#else
         int res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
+#endif
         if (active && res == RAY_CONTINUE && job.skip && r.phase == PH_MARCH) res = proposal_skip(r, job, pix);
         if (active && res == RAY_BRACKET) {
             // precision form: hand the crossing to the FP64 bisection pass
