@@ -142,6 +142,31 @@ __device__ __forceinline__ void renorm(float &p, int32_t &e, uint32_t &bad)
     p = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
 }
 
+// The product form's accumulated step on the negated state s = -v, with the
+// signed product (|p| is the scalar form's p; renormalisation drops the
+// sign): mt = r*s = -(r*v); s' = mt*s + mt = -(t - t*v); d = (2r)*s' + r =
+// r - 2r*v'; p' = p*d.  Round-to-nearest is symmetric, so every quantity is
+// the plain statement's value or its exact negation -- and no instruction
+// beyond the four FP32 operations is needed (no abs, no negation).
+__device__ __forceinline__ void product_step(float r, float tr, float &s, float &p)
+{
+    const float mt = r * s;
+    s = __fmaf_rn(mt, s, mt);
+    p = p * __fmaf_rn(tr, s, r);
+}
+
+// renorm with the range check folded into one unsigned maximum: a block is
+// out of range when (biased exponent - 27) > 200 as an unsigned number, so
+// the largest such value over all blocks decides (bad = mx > 200)
+__device__ __forceinline__ void renorm_max(float &p, int32_t &e, uint32_t &mx)
+{
+    const uint32_t bits = __float_as_uint(p);
+    const uint32_t ef = (bits >> 23) & 0xffu;
+    mx = max(mx, ef - 27u);
+    e += (int32_t)ef;
+    p = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+}
+
 __host__ __device__ constexpr int ctz_lcm8(int L) { return (L % 8 == 0) ? L : (L % 4 == 0) ? 2 * L : (L % 2 == 0) ? 4 * L : 8 * L; }
 template <int L>
 struct Unroll {
@@ -207,28 +232,25 @@ __device__ __forceinline__ float lambda_fixed(float x, float y, float z, const S
                 l2 += lg2_approx(fabsf(dd));
             }
         } else {
-            float p = 1.0f;
+            float p = 1.0f, sv = -v;
             int32_t e = 0;
-            uint32_t bad = 0;
+            uint32_t mx = 0;
             for (uint32_t b = 0; b < nb; b++) {
 #pragma unroll
                 for (int j = 0; j < U; j++) {
-                    v = map_step(rA[j % L], v);
-                    float dd = __fmaf_rn(mA[j % L], v, rA[j % L]);
-                    p = p * fabsf(dd);
-                    if ((j & 7) == 7) renorm(p, e, bad);
+                    product_step(rA[j % L], -mA[j % L], sv, p);
+                    if ((j & 7) == 7) renorm_max(p, e, mx);
                 }
             }
             uint32_t k = 0;
             for (uint32_t j = 0; j < rem; j++) {
                 const float r = pick((si.wA >> (2 * k)) & 3u, x, y, z, d);
                 k = (k + 1 == (uint32_t)L) ? 0 : k + 1;
-                v = map_step(r, v);
-                float dd = __fmaf_rn(-2.0f * r, v, r);
-                p = p * fabsf(dd);
-                if ((j & 7u) == 7u) renorm(p, e, bad);
+                product_step(r, 2.0f * r, sv, p);
+                if ((j & 7u) == 7u) renorm_max(p, e, mx);
             }
-            renorm(p, e, bad);
+            renorm_max(p, e, mx);
+            const uint32_t bad = mx > 200u;
             // e holds the sum of biased exponents, one bias of 127 per renorm
             const uint32_t nrenorm = A / 8 + 1;
             l2 = (float)(e - (int32_t)(127u * nrenorm)) + lg2_approx(p);
@@ -454,14 +476,15 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
             }
         }
     } else {
-        float p[K];
+        float p[K], sv[K];
         int32_t e[K];
-        uint32_t bad[K];
+        uint32_t emx[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
             p[k] = 1.0f;
+            sv[k] = -v[k];
             e[k] = 0;
-            bad[k] = 0;
+            emx[k] = 0;
         }
         for (uint32_t b = 0; b < nb; b++) {
 #pragma unroll
@@ -471,9 +494,8 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
                     const uint32_t sym = SA::at(j % L);
                     const float r = pick(sym, px[k], py[k], pz[k], d);
                     const float m = pick(sym, mx[k], my[k], mz[k], md);
-                    v[k] = map_step(r, v[k]);
-                    p[k] = p[k] * fabsf(__fmaf_rn(m, v[k], r));
-                    if ((j & 7) == 7) renorm(p[k], e[k], bad[k]);
+                    product_step(r, -m, sv[k], p[k]);
+                    if ((j & 7) == 7) renorm_max(p[k], e[k], emx[k]);
                 }
             }
         }
@@ -485,17 +507,16 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
             for (int k = 0; k < K; k++) {
                 const float r = pick(sym, px[k], py[k], pz[k], d);
                 const float m = pick(sym, mx[k], my[k], mz[k], md);
-                v[k] = map_step(r, v[k]);
-                p[k] = p[k] * fabsf(__fmaf_rn(m, v[k], r));
-                if ((j & 7u) == 7u) renorm(p[k], e[k], bad[k]);
+                product_step(r, -m, sv[k], p[k]);
+                if ((j & 7u) == 7u) renorm_max(p[k], e[k], emx[k]);
             }
         }
         const int32_t bias = (int32_t)(127u * (A / 8 + 1));
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            renorm(p[k], e[k], bad[k]);
+            renorm_max(p[k], e[k], emx[k]);
             l2[k] = (float)(e[k] - bias) + lg2_approx(p[k]);
-            if (bad[k] && !((skipped >> k) & 1u)) fallback |= 1u << k;
+            if (emx[k] > 200u && !((skipped >> k) & 1u)) fallback |= 1u << k;
         }
     }
 #pragma unroll
@@ -568,12 +589,12 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
     }
     uint64_t p = f2_pack(1.0f, 1.0f);
     int32_t e0 = 0, e1 = 0;
-    uint32_t bad0 = 0, bad1 = 0;
+    uint32_t mx0 = 0, mx1 = 0;
     auto renorm2 = [&]() {
         float a, b;
         f2_unpack(p, a, b);
-        renorm(a, e0, bad0);
-        renorm(b, e1, bad1);
+        renorm_max(a, e0, mx0);
+        renorm_max(b, e1, mx1);
         p = f2_pack(a, b);
     };
     const uint32_t nb = A / U, rem = A - nb * U;
@@ -603,8 +624,8 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
     f2_unpack(p, p0, p1);
     const int32_t bias = (int32_t)(127u * (A / 8 + 1));
     float l2[2] = {(float)(e0 - bias) + lg2_approx(p0), (float)(e1 - bias) + lg2_approx(p1)};
-    if (bad0 && !(skipped & 1u)) fallback |= 1u;
-    if (bad1 && !(skipped & 2u)) fallback |= 2u;
+    if (mx0 > 200u && !(skipped & 1u)) fallback |= 1u;
+    if (mx1 > 200u && !(skipped & 2u)) fallback |= 2u;
 #pragma unroll
     for (int k = 0; k < 2; k++) {
         const float lk = ((skipped >> k) & 1u) ? 0.0f : l2[k];
