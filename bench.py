@@ -342,6 +342,17 @@ def run_ours(args):
                "frames_per_s": world * args.steps / e2e_s,
                "call": "lyap_render_host (pinned host buffers; upload, render, download RGBA + LyapPoint, sync)"}
 
+    # how much of one frame is spent after the pixel queue drained (the tail)
+    frame.reset_stats()
+    frame.run(capi.VARIANT_PRODUCT, stream=stream, jit=jit)
+    torch.cuda.synchronize()
+    tst = frame.stats()
+    mask = (1 << 64) - 1
+    t_start, t_drain, t_end = (~int(tst[capi.STAT_T_START])) & mask, (~int(tst[capi.STAT_T_DRAIN])) & mask, \
+        int(tst[capi.STAT_T_END])
+    tail = {"frame_ms": (t_end - t_start) / 1e6, "after_queue_drained_ms": (t_end - t_drain) / 1e6,
+            "tail_frac": (t_end - t_drain) / max(1, t_end - t_start)} if t_end > t_drain > t_start else None
+
     # secondary: the dense volume sweep (HBM write-out roofline)
     volume = None
     if args.volume > 0:
@@ -389,6 +400,7 @@ def run_ours(args):
             "iters_per_frame": iters_frame,
             "samples_per_frame": int(chosen_st[capi.STAT_SAMPLES]) // args.steps,
             "hits_per_frame": int(chosen_st[capi.STAT_HITS]) // args.steps,
+            "queue_tail": tail,
             "warp_rounds": {"lane_utilisation": float(chosen_st[capi.STAT_LANE_ROUNDS]) /
                                                 max(1.0, 32.0 * float(chosen_st[capi.STAT_ROUNDS])),
                             "rounds_per_frame": int(chosen_st[capi.STAT_ROUNDS]) // args.steps,

@@ -219,7 +219,15 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_STAT_PROPOSAL_POINTS 14  /* render: points the proposal net evaluated */
 #define LYAP_STAT_NET_TIMEOUTS 15     /* tensor-core waits that ran out; the
                                           tiles concerned skip nothing */
-#define LYAP_STAT_COUNT    16
+/* render timing (%globaltimer, ns): START and DRAIN hold the bitwise NOT of
+ * the earliest warp start / the earliest moment a warp found the pixel queue
+ * empty (kept with atomicMax on ~t, so a zeroed array works); END the latest
+ * warp end.  (END - ~DRAIN) / (END - ~START) is the share of the launch spent
+ * finishing rays already started. */
+#define LYAP_STAT_T_START  16
+#define LYAP_STAT_T_DRAIN  17
+#define LYAP_STAT_T_END    18
+#define LYAP_STAT_COUNT    19
 
 /* LyapRenderExt / LyapVolumeExt flags.  Given the host copy of the sequence
  * (h_seq), the library compiles the kernels for that sequence at run time
@@ -230,6 +238,10 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_FLAG_REQUIRE_JIT 2u  /* fail (LYAP_ERR_JIT) instead of falling back */
 #define LYAP_FLAG_NO_SPECULATION 4u /* render: idle lanes do not take samples
                                        ahead for running rays (same results) */
+#define LYAP_FLAG_SPREAD_ORDER 16u /* render: the pixel queue spreads
+                                      consecutive pixels over the image
+                                      instead of scanline order (same
+                                      results; frame time within +-10%) */
 #define LYAP_FLAG_BISECT_F64  8u  /* render, precision form: instead of the
                                      reference's honing, bisect each ray's
                                      crossing [last sample above, first at or

@@ -30,6 +30,7 @@ FLAG_NO_JIT = 1
 FLAG_REQUIRE_JIT = 2
 FLAG_NO_SPECULATION = 4
 FLAG_BISECT_F64 = 8
+FLAG_SPREAD_ORDER = 16
 FORM_F64 = 2
 
 VARIANT_PLAIN = 0
@@ -41,8 +42,8 @@ MAX_LIGHTS = 16
 
 (STAT_SAMPLES, STAT_SKIPPED, STAT_MARCH, STAT_HONE, STAT_NORMAL, STAT_HITS, STAT_RAYS, STAT_FALLBACK, STAT_SPEC,
  STAT_SPEC_USED, STAT_ROUNDS, STAT_LANE_ROUNDS, STAT_MAX_ROUNDS, STAT_PROPOSAL_SKIPPED, STAT_PROPOSAL_POINTS,
- STAT_NET_TIMEOUTS) = range(16)
-STAT_COUNT = 16
+ STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END) = range(19)
+STAT_COUNT = 19
 
 NET_MAGIC = 0x4E50594C
 NET_VERSION = 1

@@ -135,6 +135,22 @@ int check_render_args(const LyapCam *cam, const LyapParams *prm, const void *seq
     return check_ext_render(ext, prm, fn);
 }
 
+// the pixel-queue stride: the integer nearest 0.618 * npix that is coprime with npix
+uint32_t queue_stride(uint32_t npix)
+{
+    if (npix < 3) return 0u;
+    uint32_t s = (uint32_t)((double)npix * 0.6180339887498949 + 0.5);
+    for (;; s++) {
+        uint32_t a = npix, b = s;
+        while (b) {
+            const uint32_t t = a % b;
+            a = b;
+            b = t;
+        }
+        if (a == 1u) return s;
+    }
+}
+
 RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
                           const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
                           uint32_t width, uint32_t height, const LyapRenderExt *ext)
@@ -154,6 +170,7 @@ RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_s
     job.height = height;
     job.light_model = ext ? ext->light_model : LYAP_LIGHT_SPOT;
     job.flags = ext ? ext->flags : 0u;
+    job.order_stride = (job.flags & LYAP_FLAG_SPREAD_ORDER) ? queue_stride(width * height) : 0u;
     return job;
 }
 

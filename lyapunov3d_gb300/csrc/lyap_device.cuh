@@ -130,16 +130,44 @@ __device__ __forceinline__ float map_step(float r, float v)
     return __fmaf_rn(-t, v, t);
 }
 
-// Block end of the product form: move the float exponent of p into e, put p
-// back into [1, 2); flag a block that ended outside [2^-100, 2^100] (an
-// intermediate product may have left the normal range) or non-finite.
-__device__ __forceinline__ void renorm(float &p, int32_t &e, uint32_t &bad)
+// The product form's running product restarts every 8 accumulation steps
+// (a block) at m * 2^100, m in [1, 2): the block's float exponent goes into an
+// integer and the mantissa carries on.  Starting at 2^100 rather than 1
+// leaves 226 octaves below for the block's factors |d| = |r (1 - 2v)|: for a
+// float v != 1/2 |1 - 2v| >= 2^-24, so eight factors with r >= 1/4 cannot
+// reach the subnormal range, and with |d| <= r <= 4 they stay below 2^117.
+// Only a zero factor (v landing on 1/2: lambda is NaN in every form) or a
+// degenerate r leaves the range; such a block ends outside [2^-112, 2^127)
+// -- a product that was subnormal after some step ends below 2^-126 * 4^7 --
+// and the sample is redone in the plain form, unless the block is known to
+// hold a zero factor (product_nan_exact).  Scaling by 2^100 is exact, so
+// every other sample's mantissas, exponents and lambda are those of a product
+// restarted at 1.
+constexpr uint32_t PRODUCT_EXP = 227u;                 // biased exponent of 2^100
+constexpr float PRODUCT_START = 1267650600228229401496703205376.0f;   // 2^100
+
+// The plain form's lambda is NaN exactly when its sum of lg2|d| is not
+// finite (kernel.cu returns NaN for a non-finite sum), i.e. when some factor
+// d is 0, infinite or NaN: a finite sum of at most 2^32 terms of magnitude
+// below 2^8 cannot overflow.  Two cases of an out-of-range product are known
+// to be such samples without redoing them:
+//  - the orbit ended non-finite (r > 4 -- a sample just outside the box, as
+//    normal estimation and the last march step take -- lets v leave [0, 1],
+//    after which it runs to -inf): the last factor was +inf or NaN;
+//  - the worst block ended at exactly 0 or subnormal ((biased exponent - 15)
+//    = ZERO_BLOCK unsigned) and every r is at least 1/4: non-zero factors
+//    cannot take the product there (above), so one factor was 0.
+constexpr uint32_t ZERO_BLOCK = 0u - 15u;
+__device__ __forceinline__ bool product_is_nan(uint32_t mx, float s_end, float x, float y, float z, float d)
 {
-    uint32_t bits = __float_as_uint(p);
-    uint32_t ef = (bits >> 23) & 0xffu;
-    bad |= (uint32_t)((ef - 27u) > 200u);
-    e += (int32_t)ef;
-    p = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+    return !f_isfinite(s_end) ||
+           (mx == ZERO_BLOCK && fminf(fminf(fabsf(x), fabsf(y)), fminf(fabsf(z), fabsf(d))) >= 0.25f);
+}
+
+// the renormalised product's mantissa in [1, 2), for the sample's one log2
+__device__ __forceinline__ float product_mantissa(float p)
+{
+    return __uint_as_float((__float_as_uint(p) & 0x007fffffu) | 0x3f800000u);
 }
 
 // The product form's accumulated step on the negated state s = -v, with the
@@ -156,15 +184,15 @@ __device__ __forceinline__ void product_step(float r, float tr, float &s, float 
 }
 
 // renorm with the range check folded into one unsigned maximum: a block is
-// out of range when (biased exponent - 27) > 200 as an unsigned number, so
-// the largest such value over all blocks decides (bad = mx > 200)
+// out of range when (biased exponent - 15) > 238 as an unsigned number, so
+// the largest such value over all blocks decides (bad = mx > 238)
 __device__ __forceinline__ void renorm_max(float &p, int32_t &e, uint32_t &mx)
 {
     const uint32_t bits = __float_as_uint(p);
     const uint32_t ef = (bits >> 23) & 0xffu;
-    mx = max(mx, ef - 27u);
+    mx = max(mx, ef - 15u);
     e += (int32_t)ef;
-    p = __uint_as_float((bits & 0x007fffffu) | 0x3f800000u);
+    p = __uint_as_float((bits & 0x007fffffu) | (PRODUCT_EXP << 23));
 }
 
 __host__ __device__ constexpr int ctz_lcm8(int L) { return (L % 8 == 0) ? L : (L % 4 == 0) ? 2 * L : (L % 2 == 0) ? 4 * L : 8 * L; }
@@ -232,7 +260,7 @@ __device__ __forceinline__ float lambda_fixed(float x, float y, float z, const S
                 l2 += lg2_approx(fabsf(dd));
             }
         } else {
-            float p = 1.0f, sv = -v;
+            float p = PRODUCT_START, sv = -v;
             int32_t e = 0;
             uint32_t mx = 0;
             for (uint32_t b = 0; b < nb; b++) {
@@ -250,10 +278,11 @@ __device__ __forceinline__ float lambda_fixed(float x, float y, float z, const S
                 if ((j & 7u) == 7u) renorm_max(p, e, mx);
             }
             renorm_max(p, e, mx);
-            const uint32_t bad = mx > 200u;
-            // e holds the sum of biased exponents, one bias of 127 per renorm
+            const uint32_t bad = mx > 238u;
+            // e holds the sum of biased exponents, one bias of PRODUCT_EXP per renorm
             const uint32_t nrenorm = A / 8 + 1;
-            l2 = (float)(e - (int32_t)(127u * nrenorm)) + lg2_approx(p);
+            l2 = (float)(e - (int32_t)(PRODUCT_EXP * nrenorm)) + lg2_approx(product_mantissa(p));
+            if (bad && product_is_nan(mx, sv, x, y, z, d)) return __int_as_float(0x7fffffff);
             if (bad) {
                 // an intermediate product may have been subnormal: redo in the plain
                 // form (the rolled evaluator: same operations, kept out of line)
@@ -288,9 +317,9 @@ __device__ __noinline__ float lambda_generic(float x, float y, float z, const Se
     if (!skipped) {
         const uint32_t kA = k;
         const float vA = v;
-        float p = 1.0f;
+        float p = PRODUCT_START;
         int32_t e = 0;
-        uint32_t bad = 0;
+        uint32_t mx = 0;
         for (uint32_t n = 0; n < si.A; n++) {
             float r = pick((uint32_t)seq[k] & 3u, x, y, z, d);
             k = (k + 1 == L) ? 0 : k + 1;
@@ -300,14 +329,15 @@ __device__ __noinline__ float lambda_generic(float x, float y, float z, const Se
                 l2 += lg2_approx(fabsf(dd));
             } else {
                 p = p * fabsf(dd);
-                if ((n & 7u) == 7u) renorm(p, e, bad);
+                if ((n & 7u) == 7u) renorm_max(p, e, mx);
             }
         }
         if (MODE == MODE_PRODUCT) {
-            renorm(p, e, bad);
+            renorm_max(p, e, mx);
             const uint32_t nrenorm = si.A / 8 + 1;
-            l2 = (float)(e - (int32_t)(127u * nrenorm)) + lg2_approx(p);
-            if (bad) {
+            l2 = (float)(e - (int32_t)(PRODUCT_EXP * nrenorm)) + lg2_approx(product_mantissa(p));
+            if (mx > 238u && product_is_nan(mx, v, x, y, z, d)) return __int_as_float(0x7fffffff);
+            if (mx > 238u) {
                 fallback = true;
                 l2 = 0.0f;
                 v = vA;
@@ -481,7 +511,7 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
         uint32_t emx[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            p[k] = 1.0f;
+            p[k] = PRODUCT_START;
             sv[k] = -v[k];
             e[k] = 0;
             emx[k] = 0;
@@ -511,12 +541,17 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
                 if ((j & 7u) == 7u) renorm_max(p[k], e[k], emx[k]);
             }
         }
-        const int32_t bias = (int32_t)(127u * (A / 8 + 1));
+        const int32_t bias = (int32_t)(PRODUCT_EXP * (A / 8 + 1));
 #pragma unroll
         for (int k = 0; k < K; k++) {
             renorm_max(p[k], e[k], emx[k]);
-            l2[k] = (float)(e[k] - bias) + lg2_approx(p[k]);
-            if (emx[k] > 200u && !((skipped >> k) & 1u)) fallback |= 1u << k;
+            l2[k] = (float)(e[k] - bias) + lg2_approx(product_mantissa(p[k]));
+            if (emx[k] > 238u && !((skipped >> k) & 1u)) {
+                if (product_is_nan(emx[k], sv[k], px[k], py[k], pz[k], d))
+                    l2[k] = __int_as_float(0x7fffffff);
+                else
+                    fallback |= 1u << k;
+            }
         }
     }
 #pragma unroll
@@ -587,7 +622,7 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
         if (!(v0 < 0.5f || v0 > 0.5f)) skipped |= 1u;
         if (!(v1 < 0.5f || v1 > 0.5f)) skipped |= 2u;
     }
-    uint64_t p = f2_pack(1.0f, 1.0f);
+    uint64_t p = f2_pack(PRODUCT_START, PRODUCT_START);
     int32_t e0 = 0, e1 = 0;
     uint32_t mx0 = 0, mx1 = 0;
     auto renorm2 = [&]() {
@@ -622,10 +657,23 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
     renorm2();
     float p0, p1;
     f2_unpack(p, p0, p1);
-    const int32_t bias = (int32_t)(127u * (A / 8 + 1));
-    float l2[2] = {(float)(e0 - bias) + lg2_approx(p0), (float)(e1 - bias) + lg2_approx(p1)};
-    if (mx0 > 200u && !(skipped & 1u)) fallback |= 1u;
-    if (mx1 > 200u && !(skipped & 2u)) fallback |= 2u;
+    const int32_t bias = (int32_t)(PRODUCT_EXP * (A / 8 + 1));
+    float l2[2] = {(float)(e0 - bias) + lg2_approx(product_mantissa(p0)),
+                   (float)(e1 - bias) + lg2_approx(product_mantissa(p1))};
+    float s_end0, s_end1;
+    f2_unpack(s, s_end0, s_end1);
+    if (mx0 > 238u && !(skipped & 1u)) {
+        if (product_is_nan(mx0, s_end0, px[0], py[0], pz[0], d))
+            l2[0] = __int_as_float(0x7fffffff);
+        else
+            fallback |= 1u;
+    }
+    if (mx1 > 238u && !(skipped & 2u)) {
+        if (product_is_nan(mx1, s_end1, px[1], py[1], pz[1], d))
+            l2[1] = __int_as_float(0x7fffffff);
+        else
+            fallback |= 2u;
+    }
 #pragma unroll
     for (int k = 0; k < 2; k++) {
         const float lk = ((skipped >> k) & 1u) ? 0.0f : l2[k];

@@ -42,6 +42,13 @@ namespace lyapgb {
 
 constexpr uint32_t FULL = 0xffffffffu;
 
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // ------------------------------------------------------ lambda evaluators
 // Any sequence: period and symbols read from device memory per warp.
 template <uint32_t MODE>
@@ -479,6 +486,18 @@ __device__ __forceinline__ int proposal_skip(Ray &r, const RenderJob &job, uint3
     }
 }
 
+// The pixel of queue position qi.  A ray's cost is set by where it meets the
+// surface, and neighbouring rays cost alike: in scanline order the last
+// pixels handed out -- the ones still running when the queue drains -- are
+// one band of the image.  With LYAP_FLAG_SPREAD_ORDER a stride near
+// 0.618 * npix, coprime with npix, spreads every 32 consecutive queue
+// positions over the whole image, so the rays left at the drain are a mix.
+// Every pixel is still computed exactly once, the same way.
+__device__ __forceinline__ uint32_t queue_pixel(uint32_t qi, uint32_t npix, uint32_t stride)
+{
+    return stride ? (uint32_t)(((uint64_t)qi * stride) % npix) : qi;
+}
+
 template <class Lam>
 __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
     render_persistent(const __grid_constant__ RenderJob job, uint32_t *__restrict__ work_counter,
@@ -497,7 +516,8 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
     Ray r;
     r.phase = PH_MARCH0;
     uint32_t pix = 0;
-    bool active = false, drained = false;
+    bool active = false, drained = false, drain_seen = false;
+    if (stats && lane == 0) atomicMax(stats + LYAP_STAT_T_START, ~global_ns());
 
     for (;;) {
         // refill the lanes whose ray has ended
@@ -510,10 +530,11 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
             if (lane == leader) base = atomicAdd(work_counter, (uint32_t)__popc(mask));
             base = __shfl_sync(FULL, base, leader);
             if (need) {
-                const uint32_t my = base + __popc(mask & ((1u << lane) - 1u));
-                if (my >= npix) {
+                const uint32_t qi = base + __popc(mask & ((1u << lane) - 1u));
+                if (qi >= npix) {
                     drained = true;
                 } else {
+                    const uint32_t my = queue_pixel(qi, npix, job.order_stride);
                     pix = my;
                     const uint32_t sx = my % job.width, sy = my / job.width;
                     if (ray_init(r, cr, job.prm, sx, sy)) {
@@ -532,6 +553,10 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
             }
         }
         const uint32_t amask = __ballot_sync(FULL, active);
+        if (stats && !drain_seen && __any_sync(FULL, drained)) {
+            drain_seen = true;
+            if (lane == 0) atomicMax(stats + LYAP_STAT_T_DRAIN, ~global_ns());
+        }
         if (amask == 0) break;
 
 #if LYAP_RENDER_PAIRS
@@ -566,6 +591,7 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
         }
     }
     flush_stats(stats, st, FULL);
+    if (stats && lane == 0) atomicMax(stats + LYAP_STAT_T_END, global_ns());
 }
 
 // ----------------------------------------------------------------- volume

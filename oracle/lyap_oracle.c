@@ -145,12 +145,16 @@ static float lyap_plain_f(float x, float y, float z, float d, uint32_t settle,
  * p is reset into [1, 2).  If a block ends with p outside [2^-100, 2^100]
  * (or NaN), an intermediate product may have left the normal range, and the
  * whole sample is recomputed in the plain form. */
+/* The product form: |d| multiplied up in blocks of 8 accumulation steps,
+ * each block starting at m * 2^100 (m in [1, 2)); at each block end the
+ * float exponent moves into an integer.  A block that ends outside
+ * [2^-112, 2^127) redoes the sample in the plain form. */
 static float lyap_product_f(float x, float y, float z, float d, uint32_t settle,
                             uint32_t accum, const int32_t *seq)
 {
     float abcd[4] = {x, y, z, d};
     uint32_t seqi = 0, n;
-    float r, t, v = 0.5f, p = 1.0f;
+    float r, t, v = 0.5f, p = 0x1p100f;
     int32_t e = 0;
     int bad = 0;
     for (n = 0; n < settle; n++) {
@@ -171,15 +175,21 @@ static float lyap_product_f(float x, float y, float z, float d, uint32_t settle,
                 uint32_t bits;
                 memcpy(&bits, &p, 4);
                 int32_t ef = (int32_t)((bits >> 23) & 0xffu);
-                if (ef < 27 || ef > 227) bad = 1;
-                e += ef - 127;
-                bits = (bits & 0x007fffffu) | 0x3f800000u;
+                if (ef < 15 || ef > 253) bad = 1;
+                e += ef - 227;
+                bits = (bits & 0x007fffffu) | (227u << 23);
                 memcpy(&p, &bits, 4);
             }
         }
     }
     if (bad)
         return lyap_plain_f(x, y, z, d, settle, accum, seq);
+    {   /* the mantissa in [1, 2) for the one log2 */
+        uint32_t bits;
+        memcpy(&bits, &p, 4);
+        bits = (bits & 0x007fffffu) | 0x3f800000u;
+        memcpy(&p, &bits, 4);
+    }
     float l2 = (float)e + log2f(p);
     if (!isfinite(l2)) return NAN;
     return (l2 * LN2F) / (float)accum;

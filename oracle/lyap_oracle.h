@@ -43,8 +43,8 @@ enum {
     ORC_PLAIN = 1,   /* the product's plain FP32 arithmetic: fma orbit,
                         sum of log2 (libm log2f), times ln2 / accum */
     ORC_PRODUCT = 2  /* the product's precision form: running FP32 product of
-                        |r(1-2x)| renormalised by exponent extraction every
-                        8 steps, one log2 at the end */
+                        |r(1-2x)| renormalised to [2^100, 2^101) by exponent
+                        extraction every 8 steps, one log2 at the end */
 };
 
 #define ORC_HONE_CAP 256

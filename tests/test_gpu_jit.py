@@ -126,3 +126,28 @@ def test_speculation_changes_nothing(dev, jit):
     assert st0[capi.STAT_SPEC] == 0 and st1[capi.STAT_SPEC] > 0
     assert st1[capi.STAT_SAMPLES] == st0[capi.STAT_SAMPLES]
     assert 0 < st1[capi.STAT_SPEC_USED] <= st1[capi.STAT_SPEC]
+
+
+@pytest.mark.parametrize("jit", [False, True])
+def test_spread_queue_order_changes_nothing(dev, jit):
+    """The pixel queue's spread order against scanline order (default): same
+    pixels, points, per-pixel counts and sample totals; the frame timing
+    statistics are filled in both."""
+    wl = scenes.small_render(96)
+    f = DeviceFrame(wl, device=dev, counts=True)
+    f.run(capi.VARIANT_PRODUCT, jit=jit, flags=capi.FLAG_SPREAD_ORDER)
+    rgba, pts, cnt = f.d_rgba.clone(), f.d_points.clone(), f.d_counts.clone()
+    st0 = f.stats()
+    f.reset_stats()
+    f.d_counts.zero_()
+    f.run(capi.VARIANT_PRODUCT, jit=jit)
+    torch.cuda.synchronize()
+    st1 = f.stats()
+    assert torch.equal(f.d_rgba, rgba)
+    assert torch.equal(_bits(f.d_points), _bits(pts))
+    assert torch.equal(f.d_counts, cnt)
+    assert st1[capi.STAT_SAMPLES] == st0[capi.STAT_SAMPLES]
+    mask = (1 << 64) - 1
+    for st in (st0, st1):
+        t0, td, te = (~int(st[capi.STAT_T_START])) & mask, (~int(st[capi.STAT_T_DRAIN])) & mask, int(st[capi.STAT_T_END])
+        assert 0 < t0 <= td <= te

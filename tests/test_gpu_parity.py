@@ -59,6 +59,29 @@ def test_volume_64_vs_oracle(dev, oracle, variant, mode, tol):
     assert st[capi.STAT_SAMPLES] == 64 ** 3
 
 
+@pytest.mark.parametrize("jit", [False, True])
+def test_product_out_of_range_blocks_are_nan_without_redo(dev, oracle, jit):
+    """Points just outside [2, 4] (r > 4: the orbit escapes to -inf) and
+    orbits that land on 1/2 (a zero factor) give NaN in the plain form; the
+    product form finds them NaN from its own state, with no plain redo
+    (LYAP_STAT_FALLBACK stays 0), and otherwise matches the oracle."""
+    prm = scenes.make_params(200, 1000)
+    wl = scenes.VolumeWorkload("edge", (32, 32, 32), (1.95, 1.95, 1.95), (4.2, 4.2, 4.2), "AACACBACCAAB", prm)
+    dv = DeviceVolume(wl, device=dev)
+    dv.run(capi.VARIANT_PLAIN, jit=jit)
+    plain = dv.values()
+    dv.reset_stats()
+    dv.run(capi.VARIANT_PRODUCT, jit=jit)
+    prod = dv.values()
+    st = dv.stats()
+    ref = oracle.volume(ORC_PRODUCT, 32, 32, 32, prm, dv.seq, lo=wl.lo, hi=wl.hi)
+    assert np.isnan(plain).mean() > 0.05
+    assert _nan_equal_mask(prod, plain)
+    assert _nan_equal_mask(prod, ref)
+    assert _maxdiff(prod, ref) <= LAM_TOL_PRODUCT
+    assert st[capi.STAT_FALLBACK] == 0
+
+
 def test_volume_golden_reference(dev, golden):
     """kernel_calc_volume's 32^3 sweep over [0, 4) against the reference's own host build."""
     _, g = golden
