@@ -93,7 +93,7 @@ struct Entry {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t render[2] = {nullptr, nullptr};   // [mode]
     cudaKernel_t volume[2] = {nullptr, nullptr};
-    int render_blocks_per_sm[64] = {0};
+    int render_blocks_per_sm[2][64] = {};   // per lambda form and device
     std::string log;
     double compile_ms = 0;
 };
@@ -112,24 +112,26 @@ bool jit_disabled_by_env()
 
 // Resident render blocks per SM the specialised kernel is compiled for
 // (its register cap); LYAP_JIT_RENDER_BLOCKS=4..8 overrides the default.
-// paired rounds in the specialised render (LYAP_RENDER_PAIRS): environment
-// LYAP_JIT_PAIRS=0/1 overrides the default
-int jit_render_pairs()
+// the lambda forms (the kernels' MODE_PLAIN / MODE_PRODUCT; e->render[mode])
+constexpr uint32_t kModePlain = 0, kModeProduct = 1;
+
+// paired rounds in the specialised render of lambda form `mode`: environment
+// LYAP_JIT_PAIRS=0/1 overrides the default for both forms
+int jit_render_pairs(uint32_t mode)
 {
     const char *v = getenv("LYAP_JIT_PAIRS");
     if (v && (v[0] == '0' || v[0] == '1')) return v[0] - '0';
-    return LYAP_JIT_RENDER_PAIRS;
+    return mode == kModeProduct ? LYAP_JIT_RENDER_PAIRS_PRODUCT : LYAP_JIT_RENDER_PAIRS_PLAIN;
 }
 
-int jit_render_min_blocks()
+int jit_render_min_blocks(uint32_t mode)
 {
     const char *v = getenv("LYAP_JIT_RENDER_BLOCKS");
     if (v) {
         const int n = atoi(v);
         if (n >= 2 && n <= 16) return n;
     }
-    // two samples per lane need ~96 registers: 5 blocks of 128 threads per SM
-    return jit_render_pairs() ? LYAP_JIT_RENDER_MIN_BLOCKS - 1 : LYAP_JIT_RENDER_MIN_BLOCKS;
+    return jit_render_pairs(mode) ? LYAP_JIT_RENDER_MIN_BLOCKS_PAIRS : LYAP_JIT_RENDER_MIN_BLOCKS;
 }
 
 std::string hex64(uint64_t v)
@@ -189,11 +191,15 @@ void compile_entry(Entry &e, const Spec &s)
         return;
     }
     for (auto &n : names) N.add_name(prog, n.c_str());
-    const std::string rmin = "-DLYAP_RENDER_MIN_BLOCKS=" + std::to_string(jit_render_min_blocks());
+    const std::string rmin0 = "-DLYAP_RENDER_MIN_BLOCKS_PLAIN=" + std::to_string(jit_render_min_blocks(kModePlain));
+    const std::string rmin1 =
+        "-DLYAP_RENDER_MIN_BLOCKS_PRODUCT=" + std::to_string(jit_render_min_blocks(kModeProduct));
     const std::string vmin = "-DLYAP_VOLUME_MIN_BLOCKS=" + std::to_string(LYAP_JIT_VOLUME_MIN_BLOCKS);
-    const std::string pairs = "-DLYAP_RENDER_PAIRS=" + std::to_string(jit_render_pairs());
+    const std::string pairs0 = "-DLYAP_RENDER_PAIRS_PLAIN=" + std::to_string(jit_render_pairs(kModePlain));
+    const std::string pairs1 = "-DLYAP_RENDER_PAIRS_PRODUCT=" + std::to_string(jit_render_pairs(kModeProduct));
     const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-fmad=false", "-lineinfo",
-                          "--ptxas-options=-v", rmin.c_str(), vmin.c_str(), pairs.c_str()};
+                          "--ptxas-options=-v", rmin0.c_str(), rmin1.c_str(), vmin.c_str(), pairs0.c_str(),
+                          pairs1.c_str()};
     r = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
     size_t ls = 0;
     N.log_size(prog, &ls);
@@ -299,11 +305,11 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
         cudaGetDevice(&dev);
         {
             std::lock_guard<std::mutex> lock(g_mu);
-            int &cached = e->render_blocks_per_sm[dev & 63];
+            int &cached = e->render_blocks_per_sm[mode & 1u][dev & 63];
             if (!cached) {
                 if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)e->render[mode], (int)threads,
                                                                   0) != cudaSuccess || nb <= 0)
-                    nb = jit_render_min_blocks();
+                    nb = jit_render_min_blocks(mode);
                 cached = nb;
             }
             nb = cached;

@@ -14,8 +14,14 @@
 // 256 threads per SM).
 #define LYAP_JIT_MAX_PERIOD 32
 #define LYAP_JIT_RENDER_MIN_BLOCKS 6
-// paired rounds (two samples per lane, packed FP32 pairs) in the specialised render
-#define LYAP_JIT_RENDER_PAIRS 0
+// paired rounds (two samples per lane, packed FP32 pairs) in the specialised
+// product-form render: 5-10 % faster 1080p frames than one sample per lane
+// at 6 blocks/SM; with 4 blocks/SM (up to 128 registers) 1-4 % faster than
+// with 5 or 6.  The plain form is MUFU-bound: packing gains it nothing and
+// the lower occupancy costs it, so it keeps one sample per lane.
+#define LYAP_JIT_RENDER_PAIRS_PRODUCT 1
+#define LYAP_JIT_RENDER_PAIRS_PLAIN 0
+#define LYAP_JIT_RENDER_MIN_BLOCKS_PAIRS 4
 #define LYAP_RENDER_THREADS_JIT 128
 #define LYAP_JIT_VOLUME_K 2
 #define LYAP_JIT_VOLUME_MIN_BLOCKS 4

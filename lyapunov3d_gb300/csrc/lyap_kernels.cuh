@@ -28,8 +28,19 @@
 #ifndef LYAP_RENDER_MIN_BLOCKS
 #define LYAP_RENDER_MIN_BLOCKS 4
 #endif
-#ifndef LYAP_RENDER_PAIRS
-#define LYAP_RENDER_PAIRS 0
+// per lambda form: paired rounds (two samples per lane, sample_round_pair)
+// and the resident blocks per SM the render is compiled for
+#ifndef LYAP_RENDER_PAIRS_PRODUCT
+#define LYAP_RENDER_PAIRS_PRODUCT 0
+#endif
+#ifndef LYAP_RENDER_PAIRS_PLAIN
+#define LYAP_RENDER_PAIRS_PLAIN 0
+#endif
+#ifndef LYAP_RENDER_MIN_BLOCKS_PRODUCT
+#define LYAP_RENDER_MIN_BLOCKS_PRODUCT LYAP_RENDER_MIN_BLOCKS
+#endif
+#ifndef LYAP_RENDER_MIN_BLOCKS_PLAIN
+#define LYAP_RENDER_MIN_BLOCKS_PLAIN LYAP_RENDER_MIN_BLOCKS
 #endif
 #ifndef LYAP_VOLUME_THREADS
 #define LYAP_VOLUME_THREADS 256
@@ -53,6 +64,7 @@ __device__ __forceinline__ unsigned long long global_ns()
 // Any sequence: period and symbols read from device memory per warp.
 template <uint32_t MODE>
 struct RuntimeLambda {
+    static constexpr uint32_t mode = MODE;
     SeqInfo si;
     __device__ __forceinline__ RuntimeLambda(const int32_t *seq, uint32_t period, const LyapParams &prm)
         : si(seq_setup(seq, period, prm)) {}
@@ -82,6 +94,7 @@ struct RuntimeLambda {
 // instead, so a stale specialisation can cost speed but never correctness.
 template <uint32_t MODE, uint32_t OA, class SS, class SA>
 struct ConstLambda {
+    static constexpr uint32_t mode = MODE;
     SeqInfo si;
     bool match;
     __device__ __forceinline__ ConstLambda(const int32_t *seq, uint32_t period, const LyapParams &prm)
@@ -321,7 +334,7 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     return res;
 }
 
-// Paired rounds (LYAP_RENDER_PAIRS): every lane evaluates two lambda samples
+// Paired rounds (RenderTuning::pairs): every lane evaluates two lambda samples
 // per round as one packed evaluation (Lam::eval<2>; the product form runs both
 // on FP32 pairs, fma.rn.f32x2).  Slot 0 is what sample_round evaluates; slot 1
 // is the same ray's next sample when its position is already known -- the
@@ -499,7 +512,14 @@ __device__ __forceinline__ uint32_t queue_pixel(uint32_t qi, uint32_t npix, uint
 }
 
 template <class Lam>
-__global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
+struct RenderTuning {
+    static constexpr bool product = Lam::mode == MODE_PRODUCT;
+    static constexpr bool pairs = product ? LYAP_RENDER_PAIRS_PRODUCT != 0 : LYAP_RENDER_PAIRS_PLAIN != 0;
+    static constexpr int min_blocks = product ? LYAP_RENDER_MIN_BLOCKS_PRODUCT : LYAP_RENDER_MIN_BLOCKS_PLAIN;
+};
+
+template <class Lam>
+__global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_blocks)
     render_persistent(const __grid_constant__ RenderJob job, uint32_t *__restrict__ work_counter,
                       unsigned long long *__restrict__ stats)
 {
@@ -559,11 +579,11 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, LYAP_RENDER_MIN_BLOCKS)
         }
         if (amask == 0) break;
 
-#if LYAP_RENDER_PAIRS
-        int res = sample_round_pair(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, st);
-#else
-        int res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
-#endif
+        int res;
+        if constexpr (RenderTuning<Lam>::pairs)
+            res = sample_round_pair(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, st);
+        else
+            res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
         if (active && res == RAY_CONTINUE && job.skip && r.phase == PH_MARCH) res = proposal_skip(r, job, pix);
         if (active && res == RAY_BRACKET) {
             // precision form: hand the crossing to the FP64 bisection pass

@@ -1,6 +1,7 @@
 """The specialised render with paired rounds (two samples per lane per round
-on packed FP32 pairs; LYAP_JIT_PAIRS=1, read once per process) gives the
-same frame, bit for bit, as the precompiled render."""
+on packed FP32 pairs, the default) and with one sample per lane
+(LYAP_JIT_PAIRS=0, read once per process) gives the same frame, bit for bit,
+as the precompiled render."""
 import os
 import subprocess
 import sys
@@ -30,8 +31,9 @@ print("PAIRS-OK")
 """
 
 
-def test_paired_rounds_bit_identical():
+@pytest.mark.parametrize("pairs", ["1", "0"])
+def test_paired_rounds_bit_identical(pairs):
     pytest.importorskip("torch")
-    env = dict(os.environ, LYAP_JIT_PAIRS="1")
+    env = dict(os.environ, LYAP_JIT_PAIRS=pairs)
     r = subprocess.run([sys.executable, "-c", SCRIPT, ROOT], env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and "PAIRS-OK" in r.stdout, r.stderr[-3000:]
