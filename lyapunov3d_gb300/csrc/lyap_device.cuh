@@ -428,6 +428,10 @@ template <class SS, class SA>
 __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const float (&py)[2], const float (&pz)[2],
                                                 float d, uint32_t S, uint32_t A, float (&out)[2],
                                                 uint32_t &skipped, uint32_t &fallback);
+// the product form's rare redo of a sample in the plain form, kept out of
+// line so that its unrolled loops stay out of the kernels' hot code
+template <class SS, class SA>
+__device__ __noinline__ float lambda_const_plain_redo(float x, float y, float z, float d, uint32_t S, uint32_t A);
 
 // K samples (px[k], py[k], pz[k]) with the settle symbols SS and the
 // accumulation symbols SA (SS rotated by settle mod L).  Same arithmetic as
@@ -564,14 +568,20 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
 #pragma unroll
         for (int k = 0; k < K; k++) {
             if ((fallback >> k) & 1u) {
-                const float qx[1] = {px[k]}, qy[1] = {py[k]}, qz[1] = {pz[k]};
-                float o[1];
-                uint32_t sk, fb;
-                lambda_const<MODE_PLAIN, 1, SS, SA>(qx, qy, qz, d, S, A, o, sk, fb);
-                out[k] = o[0];
+                out[k] = lambda_const_plain_redo<SS, SA>(px[k], py[k], pz[k], d, S, A);
             }
         }
     }
+}
+
+template <class SS, class SA>
+__device__ __noinline__ float lambda_const_plain_redo(float x, float y, float z, float d, uint32_t S, uint32_t A)
+{
+    const float qx[1] = {x}, qy[1] = {y}, qz[1] = {z};
+    float o[1];
+    uint32_t sk, fb;
+    lambda_const<MODE_PLAIN, 1, SS, SA>(qx, qy, qz, d, S, A, o, sk, fb);
+    return o[0];
 }
 
 // The product form for two samples at once on packed FP32 pairs.  The
@@ -683,11 +693,7 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
 #pragma unroll
         for (int k = 0; k < 2; k++) {
             if ((fallback >> k) & 1u) {
-                const float qx[1] = {px[k]}, qy[1] = {py[k]}, qz[1] = {pz[k]};
-                float o[1];
-                uint32_t sk, fb;
-                lambda_const<MODE_PLAIN, 1, SS, SA>(qx, qy, qz, d, S, A, o, sk, fb);
-                out[k] = o[0];
+                out[k] = lambda_const_plain_redo<SS, SA>(px[k], py[k], pz[k], d, S, A);
             }
         }
     }
