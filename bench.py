@@ -140,6 +140,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(values, world, device=None):
+    """Element-wise maximum of `values` over the ranks of the default process
+    group (the slowest rank's times); `values` itself at world size 1."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
+def whole_job_rate(world, units_per_step, steps, seconds):
+    """Replicas: every rank does `units_per_step` per step, so the job's rate is
+    world x units x steps over the slowest rank's time (in G units/s)."""
+    return world * units_per_step * steps / seconds / 1e9
+
+
 # --------------------------------------------------------------- CPU arms
 def cpu_render_rate(wl, seconds, threads=0):
     """The reference algorithm (oracle restatement of the reference's own
@@ -291,16 +309,10 @@ def run_ours(args):
     lam_diff = {"max_abs": float(dl.max()) if dl.size else 0.0, "mean_abs": float(dl.mean()) if dl.size else 0.0}
 
     # max over ranks
-    t_chosen = chosen_ms
-    t_plain = plain_ms
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_chosen, t_plain], dtype=torch.float64, device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_chosen, t_plain = float(tt[0]), float(tt[1])
+    t_chosen, t_plain = max_over_ranks([chosen_ms, plain_ms], world, dev)
 
-    value = world * iters_frame * args.steps / (t_chosen * 1e-3) / 1e9
-    plain_value = world * plain_iters_frame * args.steps / (t_plain * 1e-3) / 1e9
+    value = whole_job_rate(world, iters_frame, args.steps, t_chosen * 1e-3)
+    plain_value = whole_job_rate(world, plain_iters_frame, args.steps, t_plain * 1e-3)
     kernel_ms = statistics.mean(chosen_times)
     achieved = iters_frame / (kernel_ms * 1e-3) / 1e9
     # FP32-pipe bound of the chosen (product) form: 2 FP32 ops per settle step,
@@ -331,12 +343,8 @@ def run_ours(args):
             capi.render_host(frame.cam, frame.prm, frame.seq, frame.lights, wl.width, wl.height, ext=ext,
                              stream=stream, rgba=rgba_h, points=pts_h)
             e2e_s += time.perf_counter() - t0
-        if world > 1:
-            import torch.distributed as dist
-            tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_s = float(tt[0])
-        e2e = {"value": world * iters_frame * args.steps / e2e_s / 1e9, "unit": "G iters/s",
+        e2e_s = max_over_ranks([e2e_s], world, dev)[0]
+        e2e = {"value": whole_job_rate(world, iters_frame, args.steps, e2e_s), "unit": "G iters/s",
                "h2d_bytes_per_step": int(frame.seq.nbytes + 224 * len(frame.lights)),
                "d2h_bytes_per_step": int(npix * 4 + npix * 36),
                "frames_per_s": world * args.steps / e2e_s,

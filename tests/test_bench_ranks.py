@@ -1,0 +1,66 @@
+"""bench.py's multi-GPU logic (replicas: no data-path collective) on two gloo
+ranks on the CPU: the slowest rank's times decide, the job's rate counts every
+rank's work, and the reference arm runs on rank 0 only."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import torch.distributed as dist
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        w, r, _ = bench.dist_env()
+        times = bench.max_over_ranks([10.0 + rank, 20.0 - rank, 0.5 * rank], w)
+        out.put((r, w, times))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_max_over_ranks_two_gloo_ranks():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [g[0] for g in got] == [0, 1]
+    for _, w, times in got:
+        assert w == 2
+        assert times == [11.0, 20.0, 0.5]
+
+
+def test_whole_job_rate_and_single_rank():
+    import bench
+    assert bench.max_over_ranks([3.0, 4.0], 1) == [3.0, 4.0]
+    # 2 replicas, 1e9 iterations per frame, 5 frames in 2.5 s on the slowest rank
+    assert bench.whole_job_rate(2, 1e9, 5, 2.5) == pytest.approx(4.0)
+
+
+def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
+    import bench
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference"])
+    bench.run_reference_arm(bench.parse_args())
+    assert capsys.readouterr().out == ""
