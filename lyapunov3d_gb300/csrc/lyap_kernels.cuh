@@ -580,10 +580,16 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
         if (amask == 0) break;
 
         int res;
-        if constexpr (RenderTuning<Lam>::pairs)
-            res = sample_round_pair(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, st);
-        else
+        // paired rounds take a ray's next march sample only with a fixed step:
+        // with a proposal's skips the second slot would idle, so one per lane
+        if constexpr (RenderTuning<Lam>::pairs) {
+            if (job.skip == nullptr)
+                res = sample_round_pair(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, st);
+            else
+                res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
+        } else {
             res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
+        }
         if (active && res == RAY_CONTINUE && job.skip && r.phase == PH_MARCH) res = proposal_skip(r, job, pix);
         if (active && res == RAY_BRACKET) {
             // precision form: hand the crossing to the FP64 bisection pass
