@@ -135,22 +135,6 @@ int check_render_args(const LyapCam *cam, const LyapParams *prm, const void *seq
     return check_ext_render(ext, prm, fn);
 }
 
-// the pixel-queue stride: the integer nearest 0.618 * npix that is coprime with npix
-uint32_t queue_stride(uint32_t npix)
-{
-    if (npix < 3) return 0u;
-    uint32_t s = (uint32_t)((double)npix * 0.6180339887498949 + 0.5);
-    for (;; s++) {
-        uint32_t a = npix, b = s;
-        while (b) {
-            const uint32_t t = a % b;
-            a = b;
-            b = t;
-        }
-        if (a == 1u) return s;
-    }
-}
-
 RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
                           const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
                           uint32_t width, uint32_t height, const LyapRenderExt *ext)
@@ -170,7 +154,6 @@ RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_s
     job.height = height;
     job.light_model = ext ? ext->light_model : LYAP_LIGHT_SPOT;
     job.flags = ext ? ext->flags : 0u;
-    job.order_stride = (job.flags & LYAP_FLAG_SPREAD_ORDER) ? queue_stride(width * height) : 0u;
     return job;
 }
 
@@ -210,11 +193,12 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     RenderJob job = make_job(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext);
-    // scratch: the pixel queue's counter, stream-ordered so concurrent calls
-    // on different streams each get their own
-    // precision form with FP64 bisection: also the per-pixel crossing
-    // brackets and the list of pixels that crossed (scratch of the two passes)
-    // learned proposal: the net, the crossing rays and the per-pixel segment bits
+    // scratch, stream-ordered so concurrent calls on different streams each
+    // get their own: a 256-byte header (the queue's counter, the ray list's
+    // length), the list of rays that meet the box (ray_list); with FP64
+    // bisection also the per-pixel crossing brackets and the list of pixels
+    // that crossed (scratch of the two passes); with a learned proposal the
+    // net, the crossing rays and the per-pixel segment bits
     const bool bisect = ext && (ext->flags & LYAP_FLAG_BISECT_F64);
     const size_t npix = (size_t)width * height;
     const LyapNet *net = ext_proposal(ext);
@@ -223,13 +207,19 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     if (net && proposal_segments(*prm, seg_len, &words) == 0) net = nullptr;
     const size_t bisect_bytes = bisect ? 256 + (((npix + 1) * sizeof(uint32_t) + 255) & ~(size_t)255) +
                                              npix * 2 * sizeof(float)
-                                       : sizeof(uint32_t);
+                                       : 256;
     const size_t prop_off = (bisect_bytes + 255) & ~(size_t)255;
-    const size_t scratch = net ? prop_off + proposal_scratch_bytes(npix, words) : bisect_bytes;
+    const size_t prop_end = net ? prop_off + proposal_scratch_bytes(npix, words) : bisect_bytes;
+    const size_t list_off = (prop_end + 255) & ~(size_t)255;
+    const size_t scratch = list_off + npix * sizeof(uint32_t);
     uint32_t *d_counter = nullptr;
     cudaError_t e = cudaMallocAsync((void **)&d_counter, scratch, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: scratch allocation");
-    e = cudaMemsetAsync(d_counter, 0, sizeof(uint32_t), s);
+    e = cudaMemsetAsync(d_counter, 0, 2 * sizeof(uint32_t), s);
+    job.list = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(d_counter) + list_off);
+    job.list_count = d_counter + 1;
+    if (e == cudaSuccess)
+        e = launch_ray_list(job, const_cast<uint32_t *>(job.list), d_counter + 1, ext ? ext->d_stats : nullptr, s);
     if (e == cudaSuccess && bisect) {
         char *base = reinterpret_cast<char *>(d_counter);
         job.hits = reinterpret_cast<uint32_t *>(base + 256);

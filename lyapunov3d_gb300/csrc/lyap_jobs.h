@@ -34,9 +34,10 @@ struct RenderJob {
     uint32_t skip_segments;      // segments covered by the bits (later samples are always evaluated)
     uint32_t seg_len;            // march samples per segment
     uint32_t skip_dilate;        // 1: a segment is skipped only if its neighbours' bits are set too
-    // the queue hands out pixel (i * order_stride) mod (width*height) as its
-    // i-th pixel (order_stride coprime with the pixel count; 0: i itself)
-    uint32_t order_stride;
+    // the rays that meet the box, listed by ray_list (null: the queue runs
+    // over every pixel); the render's queue hands out list[i]
+    const uint32_t *list;
+    const uint32_t *list_count;  // device: entries in list
 };
 
 struct VolumeJob {

@@ -499,16 +499,30 @@ __device__ __forceinline__ int proposal_skip(Ray &r, const RenderJob &job, uint3
     }
 }
 
-// The pixel of queue position qi.  A ray's cost is set by where it meets the
+// Queue position qi -> entry.  A ray's cost is set by where it meets the
 // surface, and neighbouring rays cost alike: in scanline order the last
-// pixels handed out -- the ones still running when the queue drains -- are
-// one band of the image.  With LYAP_FLAG_SPREAD_ORDER a stride near
-// 0.618 * npix, coprime with npix, spreads every 32 consecutive queue
-// positions over the whole image, so the rays left at the drain are a mix.
-// Every pixel is still computed exactly once, the same way.
-__device__ __forceinline__ uint32_t queue_pixel(uint32_t qi, uint32_t npix, uint32_t stride)
+// entries handed out -- the rays still running when the queue drains -- are
+// one band of the image.  With LYAP_FLAG_SPREAD_ORDER a stride near 0.618 n,
+// coprime with the queue length n, spreads every 32 consecutive positions
+// over the whole image.  Every entry is still taken exactly once.
+__host__ __device__ inline uint32_t coprime_stride(uint32_t n)
 {
-    return stride ? (uint32_t)(((uint64_t)qi * stride) % npix) : qi;
+    if (n < 3u) return 0u;
+    uint32_t s = (uint32_t)((double)n * 0.6180339887498949 + 0.5);
+    for (;; s++) {
+        uint32_t a = n, b = s;
+        while (b) {
+            const uint32_t t = a % b;
+            a = b;
+            b = t;
+        }
+        if (a == 1u) return s;
+    }
+}
+
+__device__ __forceinline__ uint32_t queue_entry(uint32_t qi, uint32_t n, uint32_t stride)
+{
+    return stride ? (uint32_t)(((uint64_t)qi * stride) % n) : qi;
 }
 
 template <class Lam>
@@ -524,7 +538,9 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
                       unsigned long long *__restrict__ stats)
 {
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t npix = job.width * job.height;
+    // the queue: the listed rays that meet the box, or every pixel
+    const uint32_t nq = job.list ? *job.list_count : job.width * job.height;
+    const uint32_t stride = (job.flags & LYAP_FLAG_SPREAD_ORDER) ? coprime_stride(nq) : 0u;
     const Lam lam(job.seq, job.seq_period, job.prm);
     const CamRays cr = cam_rays(job.cam);
     // march positions are known ahead only with a fixed step length
@@ -551,10 +567,11 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
             base = __shfl_sync(FULL, base, leader);
             if (need) {
                 const uint32_t qi = base + __popc(mask & ((1u << lane) - 1u));
-                if (qi >= npix) {
+                if (qi >= nq) {
                     drained = true;
                 } else {
-                    const uint32_t my = queue_pixel(qi, npix, job.order_stride);
+                    const uint32_t e = queue_entry(qi, nq, stride);
+                    const uint32_t my = job.list ? job.list[e] : e;
                     pix = my;
                     const uint32_t sx = my % job.width, sy = my / job.width;
                     if (ray_init(r, cr, job.prm, sx, sy)) {

@@ -40,6 +40,57 @@ cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_
     return cudaGetLastError();
 }
 
+// The pre-pass of the render: every pixel's ray is set up once; a ray that
+// misses the box is finished here (exactly as the render finishes one), a ray
+// that meets it is appended to `list` (one atomic per block of 256 pixels,
+// pixel order within a block).  The render's queue then walks the list only:
+// handing out runs of missing rays one atomic at a time stalled every warp
+// of a frame with a sky band at the end of its scanline order.
+__global__ void __launch_bounds__(256) ray_list(const __grid_constant__ RenderJob job, uint32_t *__restrict__ list,
+                                                uint32_t *__restrict__ count, unsigned long long *__restrict__ stats)
+{
+    __shared__ uint32_t warp_n[8], block_base;
+    const uint32_t npix = job.width * job.height;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const CamRays cr = cam_rays(job.cam);
+    LaneStats st = {};
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool cross = false;
+    if (i < npix) {
+        Ray r;
+        r.phase = PH_MARCH0;
+        if (ray_init(r, cr, job.prm, i % job.width, i / job.width)) {
+            cross = true;
+        } else {
+            r.nm = r.nh = r.ns = 0;
+            finish_pixel(job.rgba, job.points, job.counts, i, r, false, cr.C, job.lights, job.n_lights,
+                         job.light_model, st);
+        }
+    }
+    const uint32_t m = __ballot_sync(FULL, cross);
+    if (lane == 0) warp_n[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tot = 0;
+        for (uint32_t w = 0; w < (blockDim.x >> 5); w++) tot += warp_n[w];
+        block_base = tot ? atomicAdd(count, tot) : 0u;
+    }
+    __syncthreads();
+    uint32_t off = block_base;
+    for (uint32_t w = 0; w < warp; w++) off += warp_n[w];
+    if (cross) list[off + __popc(m & ((1u << lane) - 1u))] = i;
+    flush_stats(stats, st, FULL);
+}
+
+cudaError_t launch_ray_list(const RenderJob &job, uint32_t *list, uint32_t *count, unsigned long long *d_stats,
+                            cudaStream_t stream)
+{
+    const uint64_t npix = (uint64_t)job.width * job.height;
+    const uint32_t blocks = (uint32_t)((npix + 255) / 256);
+    ray_list<<<blocks, 256, 0, stream>>>(job, list, count, d_stats);
+    return cudaGetLastError();
+}
+
 }  // namespace lyapgb
 
 using namespace lyapgb;
