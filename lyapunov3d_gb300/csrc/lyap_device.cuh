@@ -972,10 +972,20 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
     if (!to_normal) {
         // honing condition (kernel.cu:420)
         if (r.t <= r.Qt1 && r.t >= r.Qt0 && (r.Qdt <= -r.minQdt || r.Qdt >= r.minQdt) && r.nh < HONE_CAP) {
-            r.t = r.t + r.Qdt;
-            r.P = r.P + r.QdV;
-            r.phase = PH_HONE;
-            return RAY_CONTINUE;
+            const float tn = r.t + r.Qdt;
+            const V3 Pn = r.P + r.QdV;
+            if (r.phase == PH_HONE && tn == r.t && Pn.x == r.P.x && Pn.y == r.P.y && Pn.z == r.P.z) {
+                // a step below half an ulp of t and of P (a ray grazing the box,
+                // whose step is tiny): every remaining hone step samples this
+                // same point again -- the same lambda, the same sign, no change
+                // but the count -- until the cap, so the cap is taken at once
+                r.nh = HONE_CAP;
+            } else {
+                r.t = tn;
+                r.P = Pn;
+                r.phase = PH_HONE;
+                return RAY_CONTINUE;
+            }
         }
     }
     // normal from six central differences (kernel.cu:456)
