@@ -228,6 +228,57 @@ __device__ __forceinline__ void flush_stats(unsigned long long *stats, const Lan
 }
 
 // ----------------------------------------------------------------- render
+// Hone rays with at least HONE_AHEAD steps behind them are sampled ahead
+// too: honing almost always ends within 10 steps, but a ray whose hone step
+// is below an ulp of t (a grazing ray) walks the cap of 256 steps one sample
+// per round -- the last work of many frames.  Its next positions are known
+// as long as the sign of lambda does not flip (a flip halves the step).
+constexpr uint32_t HONE_AHEAD = 12;
+
+__device__ __forceinline__ bool known_ahead(const Ray &r, bool fixed_step)
+{
+    return (fixed_step && r.phase <= PH_MARCH) || (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5) ||
+           (r.phase == PH_HONE && r.nh >= HONE_AHEAD);
+}
+
+// The sample `offset` positions ahead of the one at P: march steps and hone
+// steps added one by one as ray_advance adds them (a hone step assumes no
+// flip; the owner drops the result once its step changed), normal samples
+// by index.  `valid` is false past the last normal sample.
+__device__ __forceinline__ V3 sample_ahead(V3 P, V3 V, float dt, float mag, V3 QdV, uint32_t phase, uint32_t offset,
+                                           bool &valid)
+{
+    valid = true;
+    if (phase <= PH_MARCH) {
+        for (uint32_t j = 0; j < offset; j++) P = P + V * dt;
+        return P;
+    }
+    if (phase == PH_HONE) {
+        for (uint32_t j = 0; j < offset; j++) P = P + QdV;
+        return P;
+    }
+    const uint32_t k = phase - PH_NORM0 + offset;
+    valid = k <= 5u;
+    Ray tmp;
+    tmp.P = P;
+    tmp.mag = mag;
+    tmp.phase = PH_NORM0 + (k > 5u ? 5u : k);
+    return ray_sample_point(tmp);
+}
+
+// is the ray still where a sample taken ahead in phase `kind` at the round's
+// start (hone step qdt0) continues it?
+__device__ __forceinline__ bool still_ahead(const Ray &r, uint32_t kind, float qdt0)
+{
+    return kind == 1u ? r.phase == PH_MARCH
+                      : kind == 2u ? r.phase >= PH_NORM0 : (kind == 3u && r.phase == PH_HONE && r.Qdt == qdt0);
+}
+
+__device__ __forceinline__ uint32_t sample_kind(const Ray &r)
+{
+    return r.phase <= PH_MARCH ? 1u : r.phase >= PH_NORM0 ? 2u : 3u;
+}
+
 // One round of the render loop for a warp: every lane evaluates one lambda
 // sample -- its own ray's next one, or, when the lane has no ray and
 // speculation is allowed, a sample ahead on a ray still running in the warp --
@@ -252,7 +303,7 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     bool helper = false;
     uint32_t owner = lane, offset = 0;
     if (spec_ok && amask != FULL) {
-        const bool elig = active && (r.phase <= PH_MARCH || (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5));
+        const bool elig = active && known_ahead(r, true);
         emask = __ballot_sync(FULL, elig);
         ne = __popc(emask);
         if (ne) {
@@ -280,19 +331,13 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
         const float odt = __shfl_sync(FULL, r.dt, owner);
         const float omag = __shfl_sync(FULL, r.mag, owner);
         const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
+        V3 oQ;
+        oQ.x = __shfl_sync(FULL, r.QdV.x, owner);
+        oQ.y = __shfl_sync(FULL, r.QdV.y, owner);
+        oQ.z = __shfl_sync(FULL, r.QdV.z, owner);
         if (helper) {
-            if (ophase <= PH_MARCH) {
-                // the position after `offset` more fixed steps, added one by one as ray_advance does
-                for (uint32_t j = 0; j < offset; j++) oP = oP + oV * odt;
-                Q = oP;
-            } else {
-                Ray tmp;
-                tmp.P = oP;
-                tmp.mag = omag;
-                const uint32_t k = ophase - PH_NORM0 + offset;
-                tmp.phase = PH_NORM0 + (k > 5 ? 5 : k);
-                Q = ray_sample_point(tmp);
-            }
+            bool v;
+            Q = sample_ahead(oP, oV, odt, omag, oQ, ophase, offset, v);
             st.spec += 1;
         }
     }
@@ -303,9 +348,10 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     bool skipped, fallback;
     const float lam_v = lam(Q.x, Q.y, Q.z, skipped, fallback);
     int res = RAY_CONTINUE;
-    uint32_t kind = 0;   // 1: march, 2: normal
+    uint32_t kind = 0;   // 1: march, 2: normal, 3: hone
+    const float qdt0 = r.Qdt;
     if (active) {
-        kind = (r.phase <= PH_MARCH) ? 1u : (r.phase >= PH_NORM0 ? 2u : 0u);
+        kind = sample_kind(r);
         st.samples += 1;
         st.skipped += skipped ? 1u : 0u;
         st.fallback += fallback ? 1u : 0u;
@@ -321,8 +367,7 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
             const uint32_t src = have ? nth_set_bit(imask, rr) : lane;
             const float lj = __shfl_sync(FULL, lam_v, src);
             const uint32_t bj = __shfl_sync(FULL, sk_bits, src);
-            const bool same_phase = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
-            if (have && res == RAY_CONTINUE && same_phase) {
+            if (have && res == RAY_CONTINUE && still_ahead(r, kind, qdt0)) {
                 st.samples += 1;
                 st.skipped += bj & 1u;
                 st.fallback += (bj >> 1) & 1u;
@@ -343,23 +388,6 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
 // samples of running rays two at a time: helper (owner, j) evaluates the
 // owner's samples 2j and 2j+1 ahead.  The rays consume the results in order,
 // exactly as sample_round does one by one.
-__device__ __forceinline__ V3 sample_ahead(V3 P, V3 V, float dt, float mag, uint32_t phase, uint32_t offset,
-                                           bool &valid)
-{
-    if (phase <= PH_MARCH) {
-        for (uint32_t j = 0; j < offset; j++) P = P + V * dt;   // as ray_advance adds the steps
-        valid = true;
-        return P;
-    }
-    const uint32_t k = phase - PH_NORM0 + offset;
-    valid = k <= 5u;
-    Ray tmp;
-    tmp.P = P;
-    tmp.mag = mag;
-    tmp.phase = PH_NORM0 + (k > 5u ? 5u : k);
-    return ray_sample_point(tmp);
-}
-
 template <class Lam>
 __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, const uint32_t amask, const Lam &lam,
                                                  const LyapParams &prm, const bool fixed_step, const bool spec_ok,
@@ -367,8 +395,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
 {
     const uint32_t lane = threadIdx.x & 31u;
     // can this ray's next positions be known before its current sample's lambda?
-    const bool ahead = active && ((fixed_step && r.phase <= PH_MARCH) ||
-                                  (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5));
+    const bool ahead = active && known_ahead(r, fixed_step);
     uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
     bool helper = false;
     uint32_t owner = lane, offset = 0;
@@ -391,7 +418,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     V3 Q1 = v3(3.0f, 3.0f, 3.0f);
     if (ahead) {
         bool v;
-        Q1 = sample_ahead(r.P, r.V, r.dt, r.mag, r.phase, 1u, v);
+        Q1 = sample_ahead(r.P, r.V, r.dt, r.mag, r.QdV, r.phase, 1u, v);
     }
     if (ne) {
         V3 oP, oV;
@@ -404,10 +431,14 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
         const float odt = __shfl_sync(FULL, r.dt, owner);
         const float omag = __shfl_sync(FULL, r.mag, owner);
         const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
+        V3 oQ;
+        oQ.x = __shfl_sync(FULL, r.QdV.x, owner);
+        oQ.y = __shfl_sync(FULL, r.QdV.y, owner);
+        oQ.z = __shfl_sync(FULL, r.QdV.z, owner);
         if (helper) {
             bool v0, v1;
-            Q0 = sample_ahead(oP, oV, odt, omag, ophase, offset, v0);
-            Q1 = sample_ahead(oP, oV, odt, omag, ophase, offset + 1u, v1);
+            Q0 = sample_ahead(oP, oV, odt, omag, oQ, ophase, offset, v0);
+            Q1 = sample_ahead(oP, oV, odt, omag, oQ, ophase, offset + 1u, v1);
             st.spec += (v0 ? 1u : 0u) + (v1 ? 1u : 0u);
         }
     }
@@ -419,15 +450,15 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     uint32_t skb, fbb;
     lam.template eval<2>(qx, qy, qz, lv, skb, fbb);
     int res = RAY_CONTINUE;
-    uint32_t kind = 0;   // 1: march, 2: normal
+    uint32_t kind = 0;   // 1: march, 2: normal, 3: hone
+    const float qdt0 = r.Qdt;
     if (active) {
-        kind = (r.phase <= PH_MARCH) ? 1u : (r.phase >= PH_NORM0 ? 2u : 0u);
+        kind = sample_kind(r);
         st.samples += 1;
         st.skipped += skb & 1u;
         st.fallback += fbb & 1u;
         res = ray_advance(r, lv[0], prm, bracket_mode);
-        const bool same = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
-        if (ahead && res == RAY_CONTINUE && same) {
+        if (ahead && res == RAY_CONTINUE && still_ahead(r, kind, qdt0)) {
             st.samples += 1;
             st.skipped += (skb >> 1) & 1u;
             st.fallback += (fbb >> 1) & 1u;
@@ -447,8 +478,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
             const uint32_t b = __shfl_sync(FULL, bits, src);
 #pragma unroll
             for (int h = 0; h < 2; h++) {
-                const bool same = (kind == 1u) ? (r.phase == PH_MARCH) : (kind == 2u && r.phase >= PH_NORM0);
-                if (have && res == RAY_CONTINUE && same) {
+                if (have && res == RAY_CONTINUE && still_ahead(r, kind, qdt0)) {
                     st.samples += 1;
                     st.skipped += (b >> h) & 1u;
                     st.fallback += (b >> (2 + h)) & 1u;

@@ -151,3 +151,26 @@ def test_spread_queue_order_changes_nothing(dev, jit):
     for st in (st0, st1):
         t0, td, te = (~int(st[capi.STAT_T_START])) & mask, (~int(st[capi.STAT_T_DRAIN])) & mask, int(st[capi.STAT_T_END])
         assert 0 < t0 <= td <= te
+
+
+@pytest.mark.parametrize("jit", [False, True])
+def test_speculation_changes_nothing_full_frame(dev, jit):
+    """The 1080p bench frame with and without sampling ahead: the same pixels,
+    points and per-pixel counts.  The frame has rays that walk the hone cap
+    (grazing rays, sampled ahead in the hone phase) and rays in every phase
+    at the end of the frame."""
+    wl = scenes.full_render(1, 1920, 1080)
+    f = DeviceFrame(wl, device=dev, counts=True)
+    f.run(capi.VARIANT_PRODUCT, jit=jit, flags=capi.FLAG_NO_SPECULATION)
+    rgba, pts, cnt = f.d_rgba.clone(), f.d_points.clone(), f.d_counts.clone()
+    f.reset_stats()
+    f.d_counts.zero_()
+    f.run(capi.VARIANT_PRODUCT, jit=jit)
+    torch.cuda.synchronize()
+    st = f.stats()
+    assert torch.equal(f.d_rgba, rgba)
+    assert torch.equal(_bits(f.d_points), _bits(pts))
+    assert torch.equal(f.d_counts, cnt)
+    hone = f.counts()[..., 1]
+    assert (hone == 256).sum() > 0 and hone.max() == 256
+    assert st[capi.STAT_SPEC_USED] > 0
