@@ -430,7 +430,8 @@ def run_ours(args):
             "e2e": e2e,
             "volume": volume,
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps,
+            # per timed frame: ray_list (the pre-pass) and render_persistent
+            "gpu_launches": 2 * args.steps,
             "jit": capi.jit_info()[1].split("\n")[0] if jit else "off",
             "clocks": clocks,
         }
