@@ -208,7 +208,9 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_STAT_NORMAL   4  /* render: normal samples                      */
 #define LYAP_STAT_HITS     5  /* render: rays that hit                       */
 #define LYAP_STAT_RAYS     6  /* render: rays finished                       */
-#define LYAP_STAT_FALLBACK 7  /* product evaluations redone in plain form    */
+#define LYAP_STAT_FALLBACK 7  /* product evaluations taken again: with blocks
+                                 of 8 steps after longer blocks left the
+                                 range, or in the plain form               */
 #define LYAP_STAT_SPEC     8  /* render: samples taken ahead by idle lanes   */
 #define LYAP_STAT_SPEC_USED 9 /* render: of those, samples the rays used      */
 #define LYAP_STAT_ROUNDS   10 /* render: warp rounds (one lambda sample each) */

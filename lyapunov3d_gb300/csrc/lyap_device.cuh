@@ -130,21 +130,34 @@ __device__ __forceinline__ float map_step(float r, float v)
     return __fmaf_rn(-t, v, t);
 }
 
-// The product form's running product restarts every 8 accumulation steps
-// (a block) at m * 2^100, m in [1, 2): the block's float exponent goes into an
-// integer and the mantissa carries on.  Starting at 2^100 rather than 1
-// leaves 226 octaves below for the block's factors |d| = |r (1 - 2v)|: for a
-// float v != 1/2 |1 - 2v| >= 2^-24, so eight factors with r >= 1/4 cannot
-// reach the subnormal range, and with |d| <= r <= 4 they stay below 2^117.
-// Only a zero factor (v landing on 1/2: lambda is NaN in every form) or a
-// degenerate r leaves the range; such a block ends outside [2^-112, 2^127)
-// -- a product that was subnormal after some step ends below 2^-126 * 4^7 --
-// and the sample is redone in the plain form, unless the block is known to
-// hold a zero factor (product_nan_exact).  Scaling by 2^100 is exact, so
-// every other sample's mantissas, exponents and lambda are those of a product
-// restarted at 1.
-constexpr uint32_t PRODUCT_EXP = 227u;                 // biased exponent of 2^100
-constexpr float PRODUCT_START = 1267650600228229401496703205376.0f;   // 2^100
+// The product form multiplies the factors d of B consecutive accumulation
+// steps (a block) into a running product that restarts every block at
+// m * 2^(E-127), m in [1, 2): the block's float exponent goes into an integer
+// and the mantissa carries on.  B = 24 when the period's unrolled body
+// (max(16, lcm(L, 8)) steps) is a multiple of 24, else 16 when it is a
+// multiple of 16, else 8, so that blocks end at fixed places of the body.
+// |d| = |r (1 - 2v)| <= r <= 4 on an orbit in [0, 1], so a block stays below
+// 2^(E-126) * 4^B < 2^127 with E = 227, 221, 205 (2^100, 2^94, 2^78) for
+// B = 8, 16, 24; a product that was subnormal after some step ends below
+// 2^-126 * 4^(B-1) = 2^(2B-128), biased exponent 2B - 1.  Scaling by powers
+// of 2 is exact, so while no block leaves [2^(2B-128), 2^127) the mantissas,
+// exponents and lambda are those of a product restarted at 1 -- the same for
+// every B.  The form is defined by B = 8: a sample whose blocks of 16 or 24
+// left the range is taken again with blocks of 8 (if a block of 24 stays in
+// range, each of its blocks of 8 ends above 2^100 * 2^-159 / 4^16 = 2^-91,
+// in range too, so nothing else changes), and a sample out of range with
+// blocks of 8 goes to the plain form (below).
+__host__ __device__ constexpr uint32_t lcm8(uint32_t L)
+{
+    return (L % 8u == 0u) ? L : (L % 4u == 0u) ? 2u * L : (L % 2u == 0u) ? 4u * L : 8u * L;
+}
+__host__ __device__ constexpr uint32_t product_block(uint32_t L)
+{
+    return (lcm8(L) < 16u ? 16u : lcm8(L)) % 24u == 0u ? 24u : (lcm8(L) < 16u ? 16u : lcm8(L)) % 16u == 0u ? 16u : 8u;
+}
+__host__ __device__ constexpr uint32_t product_exp(uint32_t B) { return B == 24u ? 205u : B == 16u ? 221u : 227u; }
+__host__ __device__ constexpr uint32_t product_lo(uint32_t B) { return 2u * B - 1u; }   // lowest valid block end
+__device__ __forceinline__ float product_start(uint32_t B) { return __uint_as_float(product_exp(B) << 23); }
 
 // The plain form's lambda is NaN exactly when its sum of lg2|d| is not
 // finite (kernel.cu returns NaN for a non-finite sum), i.e. when some factor
@@ -154,15 +167,20 @@ constexpr float PRODUCT_START = 1267650600228229401496703205376.0f;   // 2^100
 //  - the orbit ended non-finite (r > 4 -- a sample just outside the box, as
 //    normal estimation and the last march step take -- lets v leave [0, 1],
 //    after which it runs to -inf): the last factor was +inf or NaN;
-//  - the worst block ended at exactly 0 or subnormal ((biased exponent - 15)
-//    = ZERO_BLOCK unsigned) and every r is at least 1/4: non-zero factors
-//    cannot take the product there (above), so one factor was 0.
+//  - B = 8, the worst block ended at exactly 0 or subnormal ((biased
+//    exponent - 15) = ZERO_BLOCK unsigned) and every r is at least 1/4: for a
+//    float v != 1/2, |1 - 2v| >= 2^-24, so eight non-zero factors take a block
+//    from 2^100 at most down to 2^100 * 2^-208 -- it had a factor 0.
 constexpr uint32_t ZERO_BLOCK = 0u - 15u;
-__device__ __forceinline__ bool product_is_nan(uint32_t mx, float s_end, float x, float y, float z, float d)
+__device__ __forceinline__ bool product_is_nan(uint32_t B, uint32_t mx, float s_end, float x, float y, float z,
+                                               float d)
 {
-    return !f_isfinite(s_end) ||
-           (mx == ZERO_BLOCK && fminf(fminf(fabsf(x), fabsf(y)), fminf(fabsf(z), fabsf(d))) >= 0.25f);
+    return !f_isfinite(s_end) || (B == 8u && mx == ZERO_BLOCK &&
+                                  fminf(fminf(fabsf(x), fabsf(y)), fminf(fabsf(z), fabsf(d))) >= 0.25f);
 }
+
+// a block out of range: (biased exponent - lo) above 253 - lo as an unsigned
+__device__ __forceinline__ bool product_bad(uint32_t B, uint32_t mx) { return mx > 253u - product_lo(B); }
 
 // the renormalised product's mantissa in [1, 2), for the sample's one log2
 __device__ __forceinline__ float product_mantissa(float p)
@@ -183,16 +201,15 @@ __device__ __forceinline__ void product_step(float r, float tr, float &s, float 
     p = p * __fmaf_rn(tr, s, r);
 }
 
-// renorm with the range check folded into one unsigned maximum: a block is
-// out of range when (biased exponent - 15) > 238 as an unsigned number, so
-// the largest such value over all blocks decides (bad = mx > 238)
-__device__ __forceinline__ void renorm_max(float &p, int32_t &e, uint32_t &mx)
+// block end with the range check folded into one unsigned maximum: the
+// largest (biased exponent - lo) over all blocks decides (product_bad)
+__device__ __forceinline__ void renorm_max(uint32_t B, float &p, int32_t &e, uint32_t &mx)
 {
     const uint32_t bits = __float_as_uint(p);
     const uint32_t ef = (bits >> 23) & 0xffu;
-    mx = max(mx, ef - 15u);
+    mx = max(mx, ef - product_lo(B));
     e += (int32_t)ef;
-    p = __uint_as_float((bits & 0x007fffffu) | (PRODUCT_EXP << 23));
+    p = __uint_as_float((bits & 0x007fffffu) | (product_exp(B) << 23));
 }
 
 __host__ __device__ constexpr int ctz_lcm8(int L) { return (L % 8 == 0) ? L : (L % 4 == 0) ? 2 * L : (L % 2 == 0) ? 4 * L : 8 * L; }
@@ -203,7 +220,7 @@ struct Unroll {
 
 template <uint32_t MODE>
 __device__ __noinline__ float lambda_generic(float x, float y, float z, const SeqInfo &si, bool &skipped,
-                                             bool &fallback);
+                                             bool &fallback, uint32_t block = 0);
 
 // lambda for a period L <= 16: whole blocks of U = lcm(L, 8) steps run fully
 // unrolled with r in registers; the < U remaining steps run rolled, taking
@@ -260,29 +277,40 @@ __device__ __forceinline__ float lambda_fixed(float x, float y, float z, const S
                 l2 += lg2_approx(fabsf(dd));
             }
         } else {
-            float p = PRODUCT_START, sv = -v;
+            constexpr uint32_t B = product_block(L);
+            static_assert(U % B == 0, "blocks end inside the unrolled body");
+            float p = product_start(B), sv = -v;
             int32_t e = 0;
             uint32_t mx = 0;
             for (uint32_t b = 0; b < nb; b++) {
 #pragma unroll
                 for (int j = 0; j < U; j++) {
                     product_step(rA[j % L], -mA[j % L], sv, p);
-                    if ((j & 7) == 7) renorm_max(p, e, mx);
+                    if (j % B == B - 1) renorm_max(B, p, e, mx);
                 }
             }
-            uint32_t k = 0;
+            uint32_t k = 0, kb = 0;
             for (uint32_t j = 0; j < rem; j++) {
                 const float r = pick((si.wA >> (2 * k)) & 3u, x, y, z, d);
                 k = (k + 1 == (uint32_t)L) ? 0 : k + 1;
                 product_step(r, 2.0f * r, sv, p);
-                if ((j & 7u) == 7u) renorm_max(p, e, mx);
+                if (++kb == B) {
+                    kb = 0;
+                    renorm_max(B, p, e, mx);
+                }
             }
-            renorm_max(p, e, mx);
-            const uint32_t bad = mx > 238u;
-            // e holds the sum of biased exponents, one bias of PRODUCT_EXP per renorm
-            const uint32_t nrenorm = A / 8 + 1;
-            l2 = (float)(e - (int32_t)(PRODUCT_EXP * nrenorm)) + lg2_approx(product_mantissa(p));
-            if (bad && product_is_nan(mx, sv, x, y, z, d)) return __int_as_float(0x7fffffff);
+            renorm_max(B, p, e, mx);
+            const bool bad = product_bad(B, mx);
+            // e holds the sum of biased exponents, one bias of product_exp(B) per renorm
+            const uint32_t nrenorm = A / B + 1;
+            l2 = (float)(e - (int32_t)(product_exp(B) * nrenorm)) + lg2_approx(product_mantissa(p));
+            if (bad && product_is_nan(B, mx, sv, x, y, z, d)) return __int_as_float(0x7fffffff);
+            if (bad && B != 8u) {
+                // blocks of 16 / 24 left the range: take the sample with blocks of 8 (out of line)
+                bool sk, fb;
+                fallback = true;
+                return lambda_generic<MODE_PRODUCT>(x, y, z, si, sk, fb, 8u);
+            }
             if (bad) {
                 // an intermediate product may have been subnormal: redo in the plain
                 // form (the rolled evaluator: same operations, kept out of line)
@@ -297,9 +325,10 @@ __device__ __forceinline__ float lambda_fixed(float x, float y, float z, const S
 }
 
 // lambda for any period: the symbol is loaded each step (uniform, L1-resident).
+// block = 0: the period's block length; 8: the defining one (a redo)
 template <uint32_t MODE>
 __device__ __noinline__ float lambda_generic(float x, float y, float z, const SeqInfo &si, bool &skipped,
-                                             bool &fallback)
+                                             bool &fallback, uint32_t block)
 {
     const float d = si.d;
     const int32_t *seq = si.seq;
@@ -317,9 +346,10 @@ __device__ __noinline__ float lambda_generic(float x, float y, float z, const Se
     if (!skipped) {
         const uint32_t kA = k;
         const float vA = v;
-        float p = PRODUCT_START;
+        const uint32_t B = block ? block : product_block(L);
+        float p = product_start(B);
         int32_t e = 0;
-        uint32_t mx = 0;
+        uint32_t mx = 0, kb = 0;
         for (uint32_t n = 0; n < si.A; n++) {
             float r = pick((uint32_t)seq[k] & 3u, x, y, z, d);
             k = (k + 1 == L) ? 0 : k + 1;
@@ -329,15 +359,24 @@ __device__ __noinline__ float lambda_generic(float x, float y, float z, const Se
                 l2 += lg2_approx(fabsf(dd));
             } else {
                 p = p * fabsf(dd);
-                if ((n & 7u) == 7u) renorm_max(p, e, mx);
+                if (++kb == B) {
+                    kb = 0;
+                    renorm_max(B, p, e, mx);
+                }
             }
         }
         if (MODE == MODE_PRODUCT) {
-            renorm_max(p, e, mx);
-            const uint32_t nrenorm = si.A / 8 + 1;
-            l2 = (float)(e - (int32_t)(PRODUCT_EXP * nrenorm)) + lg2_approx(product_mantissa(p));
-            if (mx > 238u && product_is_nan(mx, v, x, y, z, d)) return __int_as_float(0x7fffffff);
-            if (mx > 238u) {
+            renorm_max(B, p, e, mx);
+            const uint32_t nrenorm = si.A / B + 1;
+            l2 = (float)(e - (int32_t)(product_exp(B) * nrenorm)) + lg2_approx(product_mantissa(p));
+            if (product_bad(B, mx) && product_is_nan(B, mx, v, x, y, z, d)) return __int_as_float(0x7fffffff);
+            if (product_bad(B, mx) && B != 8u) {
+                // blocks of 16 / 24 left the range: take the sample with blocks of 8
+                bool sk, fb;
+                fallback = true;
+                return lambda_generic<MODE_PRODUCT>(x, y, z, si, sk, fb, 8u);
+            }
+            if (product_bad(B, mx)) {
                 fallback = true;
                 l2 = 0.0f;
                 v = vA;
@@ -432,11 +471,15 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
 // line so that its unrolled loops stay out of the kernels' hot code
 template <class SS, class SA>
 __device__ __noinline__ float lambda_const_plain_redo(float x, float y, float z, float d, uint32_t S, uint32_t A);
+// the product form's redo of a sample with the defining blocks of 8, out of line
+template <class SS, class SA>
+__device__ __noinline__ float lambda_const_block8_redo(float x, float y, float z, float d, uint32_t S, uint32_t A,
+                                                       uint32_t &fallback);
 
 // K samples (px[k], py[k], pz[k]) with the settle symbols SS and the
 // accumulation symbols SA (SS rotated by settle mod L).  Same arithmetic as
 // lambda_fixed, sample by sample.  skipped / fallback: bit k set for sample k.
-template <uint32_t MODE, int K, class SS, class SA>
+template <uint32_t MODE, int K, class SS, class SA, uint32_t BF = 0>
 __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (&py)[K], const float (&pz)[K],
                                              float d, uint32_t S, uint32_t A, float (&out)[K],
                                              uint32_t &skipped, uint32_t &fallback)
@@ -480,6 +523,7 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
     for (int k = 0; k < K; k++)
         if (!(v[k] < 0.5f || v[k] > 0.5f)) skipped |= 1u << k;
     float l2[K];
+    uint32_t redo8 = 0;   // samples to take again with blocks of 8
     const uint32_t nb = A / U, rem = A - nb * U;
     if (MODE == MODE_PLAIN) {
 #pragma unroll
@@ -510,12 +554,14 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
             }
         }
     } else {
+        constexpr uint32_t B = BF ? BF : product_block(L);
+        static_assert(U % B == 0, "blocks end inside the unrolled body");
         float p[K], sv[K];
         int32_t e[K];
         uint32_t emx[K];
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            p[k] = PRODUCT_START;
+            p[k] = product_start(B);
             sv[k] = -v[k];
             e[k] = 0;
             emx[k] = 0;
@@ -529,30 +575,34 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
                     const float r = pick(sym, px[k], py[k], pz[k], d);
                     const float m = pick(sym, mx[k], my[k], mz[k], md);
                     product_step(r, -m, sv[k], p[k]);
-                    if ((j & 7) == 7) renorm_max(p[k], e[k], emx[k]);
+                    if (j % B == B - 1) renorm_max(B, p[k], e[k], emx[k]);
                 }
             }
         }
-        uint32_t jj = 0;
+        uint32_t jj = 0, kb = 0;
         for (uint32_t j = 0; j < rem; j++) {
             const uint32_t sym = SA::at_rt(jj);
             jj = (jj + 1 == (uint32_t)L) ? 0 : jj + 1;
+            const bool end = ++kb == B;
+            if (end) kb = 0;
 #pragma unroll
             for (int k = 0; k < K; k++) {
                 const float r = pick(sym, px[k], py[k], pz[k], d);
                 const float m = pick(sym, mx[k], my[k], mz[k], md);
                 product_step(r, -m, sv[k], p[k]);
-                if ((j & 7u) == 7u) renorm_max(p[k], e[k], emx[k]);
+                if (end) renorm_max(B, p[k], e[k], emx[k]);
             }
         }
-        const int32_t bias = (int32_t)(PRODUCT_EXP * (A / 8 + 1));
+        const int32_t bias = (int32_t)(product_exp(B) * (A / B + 1));
 #pragma unroll
         for (int k = 0; k < K; k++) {
-            renorm_max(p[k], e[k], emx[k]);
+            renorm_max(B, p[k], e[k], emx[k]);
             l2[k] = (float)(e[k] - bias) + lg2_approx(product_mantissa(p[k]));
-            if (emx[k] > 238u && !((skipped >> k) & 1u)) {
-                if (product_is_nan(emx[k], sv[k], px[k], py[k], pz[k], d))
+            if (product_bad(B, emx[k]) && !((skipped >> k) & 1u)) {
+                if (product_is_nan(B, emx[k], sv[k], px[k], py[k], pz[k], d))
                     l2[k] = __int_as_float(0x7fffffff);
+                else if (B != 8u)
+                    redo8 |= 1u << k;
                 else
                     fallback |= 1u << k;
             }
@@ -572,6 +622,16 @@ __device__ __forceinline__ void lambda_const(const float (&px)[K], const float (
             }
         }
     }
+    if (MODE == MODE_PRODUCT && redo8) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            if ((redo8 >> k) & 1u) {
+                uint32_t fb = 0;
+                out[k] = lambda_const_block8_redo<SS, SA>(px[k], py[k], pz[k], d, S, A, fb);
+            }
+        }
+        fallback |= redo8;
+    }
 }
 
 template <class SS, class SA>
@@ -581,6 +641,17 @@ __device__ __noinline__ float lambda_const_plain_redo(float x, float y, float z,
     float o[1];
     uint32_t sk, fb;
     lambda_const<MODE_PLAIN, 1, SS, SA>(qx, qy, qz, d, S, A, o, sk, fb);
+    return o[0];
+}
+
+template <class SS, class SA>
+__device__ __noinline__ float lambda_const_block8_redo(float x, float y, float z, float d, uint32_t S, uint32_t A,
+                                                       uint32_t &fallback)
+{
+    const float qx[1] = {x}, qy[1] = {y}, qz[1] = {z};
+    float o[1];
+    uint32_t sk;
+    lambda_const<MODE_PRODUCT, 1, SS, SA, 8u>(qx, qy, qz, d, S, A, o, sk, fallback);
     return o[0];
 }
 
@@ -632,14 +703,16 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
         if (!(v0 < 0.5f || v0 > 0.5f)) skipped |= 1u;
         if (!(v1 < 0.5f || v1 > 0.5f)) skipped |= 2u;
     }
-    uint64_t p = f2_pack(PRODUCT_START, PRODUCT_START);
+    constexpr uint32_t B = product_block(L);
+    static_assert(U % B == 0, "blocks end inside the unrolled body");
+    uint64_t p = f2_pack(product_start(B), product_start(B));
     int32_t e0 = 0, e1 = 0;
     uint32_t mx0 = 0, mx1 = 0;
     auto renorm2 = [&]() {
         float a, b;
         f2_unpack(p, a, b);
-        renorm_max(a, e0, mx0);
-        renorm_max(b, e1, mx1);
+        renorm_max(B, a, e0, mx0);
+        renorm_max(B, b, e1, mx1);
         p = f2_pack(a, b);
     };
     const uint32_t nb = A / U, rem = A - nb * U;
@@ -650,10 +723,10 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
             const uint64_t mt = f2_mul(R[sym], s);
             s = f2_fma(mt, s, mt);
             p = f2_mul(p, f2_fma(TR[sym], s, R[sym]));
-            if ((j & 7) == 7) renorm2();
+            if (j % B == B - 1) renorm2();
         }
     }
-    uint32_t jj = 0;
+    uint32_t jj = 0, kb = 0;
     for (uint32_t j = 0; j < rem; j++) {
         const uint32_t sym = SA::at_rt(jj);
         jj = (jj + 1 == (uint32_t)L) ? 0 : jj + 1;
@@ -662,25 +735,33 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
         const uint64_t mt = f2_mul(r, s);
         s = f2_fma(mt, s, mt);
         p = f2_mul(p, f2_fma(tr, s, r));
-        if ((j & 7u) == 7u) renorm2();
+        if (++kb == B) {
+            kb = 0;
+            renorm2();
+        }
     }
     renorm2();
     float p0, p1;
     f2_unpack(p, p0, p1);
-    const int32_t bias = (int32_t)(PRODUCT_EXP * (A / 8 + 1));
+    const int32_t bias = (int32_t)(product_exp(B) * (A / B + 1));
     float l2[2] = {(float)(e0 - bias) + lg2_approx(product_mantissa(p0)),
                    (float)(e1 - bias) + lg2_approx(product_mantissa(p1))};
     float s_end0, s_end1;
     f2_unpack(s, s_end0, s_end1);
-    if (mx0 > 238u && !(skipped & 1u)) {
-        if (product_is_nan(mx0, s_end0, px[0], py[0], pz[0], d))
+    uint32_t redo8 = 0;   // samples to take again with blocks of 8
+    if (product_bad(B, mx0) && !(skipped & 1u)) {
+        if (product_is_nan(B, mx0, s_end0, px[0], py[0], pz[0], d))
             l2[0] = __int_as_float(0x7fffffff);
+        else if (B != 8u)
+            redo8 |= 1u;
         else
             fallback |= 1u;
     }
-    if (mx1 > 238u && !(skipped & 2u)) {
-        if (product_is_nan(mx1, s_end1, px[1], py[1], pz[1], d))
+    if (product_bad(B, mx1) && !(skipped & 2u)) {
+        if (product_is_nan(B, mx1, s_end1, px[1], py[1], pz[1], d))
             l2[1] = __int_as_float(0x7fffffff);
+        else if (B != 8u)
+            redo8 |= 2u;
         else
             fallback |= 2u;
     }
@@ -696,6 +777,16 @@ __device__ __forceinline__ void lambda_const_x2(const float (&px)[2], const floa
                 out[k] = lambda_const_plain_redo<SS, SA>(px[k], py[k], pz[k], d, S, A);
             }
         }
+    }
+    if (redo8) {
+#pragma unroll
+        for (int k = 0; k < 2; k++) {
+            if ((redo8 >> k) & 1u) {
+                uint32_t fb = 0;
+                out[k] = lambda_const_block8_redo<SS, SA>(px[k], py[k], pz[k], d, S, A, fb);
+            }
+        }
+        fallback |= redo8;
     }
 }
 
