@@ -405,6 +405,7 @@ def run_ours(args):
                        "l2": f"flushed between timed frames ({L2_FLUSH_BYTES >> 20} MiB write)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "frames_per_s": world * args.steps / (t_chosen * 1e-3),
+            "frame_ms": [round(t, 4) for t in chosen_times],
             "iters_per_frame": iters_frame,
             "samples_per_frame": int(chosen_st[capi.STAT_SAMPLES]) // args.steps,
             "hits_per_frame": int(chosen_st[capi.STAT_HITS]) // args.steps,
@@ -416,6 +417,7 @@ def run_ours(args):
                             "speculative_samples": int(chosen_st[capi.STAT_SPEC]) // args.steps,
                             "speculative_used": int(chosen_st[capi.STAT_SPEC_USED]) // args.steps},
             "plain": {"value": plain_value, "unit": "G iters/s", "ms_per_step": t_plain / args.steps,
+                      "frame_ms": [round(t, 4) for t in plain_times],
                       "frames_per_s": world * args.steps / (t_plain * 1e-3),
                       "roofline_frac": plain_achieved / peak_plain},
             "speedup_vs_plain": value / plain_value,

@@ -151,12 +151,29 @@ struct LaneStats {
     uint32_t prop_skip;             // march samples skipped on the learned proposal's word
 };
 
-// position of the n-th (0-based) set bit of mask; mask has more than n bits set
+// position of the n-th (0-based) set bit of mask; mask has more than n bits
+// set.  A binary search on population counts: five fixed steps, where
+// clearing the lowest bit n times took up to 31 dependent steps.
 __device__ __forceinline__ uint32_t nth_set_bit(uint32_t mask, uint32_t n)
 {
-    for (uint32_t i = 0; i < n; i++) mask &= mask - 1u;
-    return (uint32_t)(__ffs(mask) - 1);
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t w = 16; w; w >>= 1) {
+        const uint32_t c = (uint32_t)__popc(mask & ((1u << w) - 1u));
+        if (n >= c) {
+            n -= c;
+            mask >>= w;
+            pos += w;
+        }
+    }
+    return pos;
 }
+
+// Helper results of one sample round, per warp: the helper of rank k among
+// the lanes without a ray posts its lambda values and skip / fallback bits
+// in slot k; the owner of the ray reads its helpers' slots in order.  Both
+// render kernels run at most 128 threads per block (their launch bounds).
+constexpr uint32_t ROUND_WARPS = (LYAP_RENDER_THREADS > 128 ? LYAP_RENDER_THREADS : 128) / 32;
 
 __device__ __forceinline__ void store_point(LyapPoint *dst, const Ray &r, bool hit)
 {
@@ -298,10 +315,12 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
                                             const LyapParams &prm, const bool spec_ok, const bool bracket_mode,
                                             LaneStats &st)
 {
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __shared__ float slot_l[ROUND_WARPS][32];
+    __shared__ uint32_t slot_b[ROUND_WARPS][32];
     uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
     bool helper = false;
-    uint32_t owner = lane, offset = 0;
+    uint32_t owner = lane, offset = 0, rank = 0;
     if (spec_ok && amask != FULL) {
         const bool elig = active && known_ahead(r, true);
         emask = __ballot_sync(FULL, elig);
@@ -311,7 +330,7 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
             ni = __popc(imask);
             maxj = (ni + ne - 1) / ne;
             if (!active) {
-                const uint32_t rank = __popc(imask & ((1u << lane) - 1u));
+                rank = __popc(imask & ((1u << lane) - 1u));
                 owner = nth_set_bit(emask, rank % ne);
                 offset = 1 + rank / ne;
                 helper = true;
@@ -347,33 +366,37 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     st.lane_rounds += __popc(amask) + (ne ? (ni < maxj * ne ? ni : maxj * ne) : 0u);
     bool skipped, fallback;
     const float lam_v = lam(Q.x, Q.y, Q.z, skipped, fallback);
-    int res = RAY_CONTINUE;
-    uint32_t kind = 0;   // 1: march, 2: normal, 3: hone
-    const float qdt0 = r.Qdt;
-    if (active) {
-        kind = sample_kind(r);
-        st.samples += 1;
-        st.skipped += skipped ? 1u : 0u;
-        st.fallback += fallback ? 1u : 0u;
-        res = ray_advance(r, lam_v, prm, bracket_mode);
-    }
+    uint32_t bits = (skipped ? 1u : 0u) | (fallback ? 2u : 0u);
     if (ne) {
-        const bool own_elig = (emask >> lane) & 1u;
-        const uint32_t idx = __popc(emask & ((1u << lane) - 1u));
-        const uint32_t sk_bits = (skipped ? 1u : 0u) | (fallback ? 2u : 0u);
-        for (uint32_t j = 1; j <= maxj; j++) {
-            const uint32_t rr = (j - 1) * ne + idx;
-            const bool have = own_elig && rr < ni;
-            const uint32_t src = have ? nth_set_bit(imask, rr) : lane;
-            const float lj = __shfl_sync(FULL, lam_v, src);
-            const uint32_t bj = __shfl_sync(FULL, sk_bits, src);
-            if (have && res == RAY_CONTINUE && still_ahead(r, kind, qdt0)) {
-                st.samples += 1;
-                st.skipped += bj & 1u;
-                st.fallback += (bj >> 1) & 1u;
-                st.spec_used += 1;
-                res = ray_advance(r, lj, prm, bracket_mode);
-            }
+        __syncwarp();   // the owners' reads of the previous round are done
+        if (helper) {
+            slot_l[warp][rank] = lam_v;
+            slot_b[warp][rank] = bits;
+        }
+        __syncwarp();
+    }
+    int res = RAY_CONTINUE;
+    if (active) {
+        const uint32_t kind = sample_kind(r);   // 1: march, 2: normal, 3: hone
+        const float qdt0 = r.Qdt;
+        // this ray's helpers: ranks idx, idx + ne, ... below ni, one sample each
+        uint32_t idx = 0, nh = 0;
+        if (ne && ((emask >> lane) & 1u)) {
+            idx = __popc(emask & ((1u << lane) - 1u));
+            nh = idx < ni ? (ni - idx + ne - 1) / ne : 0u;
+        }
+        float l = lam_v;
+        // the own sample, then the helpers' in order while the ray continues
+        // in the phase they were taken for
+        for (uint32_t j = 0;; j++) {
+            st.samples += 1;
+            st.skipped += bits & 1u;
+            st.fallback += (bits >> 1) & 1u;
+            st.spec_used += j ? 1u : 0u;
+            res = ray_advance(r, l, prm, bracket_mode);
+            if (res != RAY_CONTINUE || j >= nh || !still_ahead(r, kind, qdt0)) break;
+            l = slot_l[warp][j * ne + idx];
+            bits = slot_b[warp][j * ne + idx];
         }
     }
     return res;
@@ -393,12 +416,14 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
                                                  const LyapParams &prm, const bool fixed_step, const bool spec_ok,
                                                  const bool bracket_mode, LaneStats &st)
 {
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    __shared__ float2 slot_l[ROUND_WARPS][32];
+    __shared__ uint32_t slot_b[ROUND_WARPS][32];
     // can this ray's next positions be known before its current sample's lambda?
     const bool ahead = active && known_ahead(r, fixed_step);
     uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
     bool helper = false;
-    uint32_t owner = lane, offset = 0;
+    uint32_t owner = lane, offset = 0, rank = 0;
     if (spec_ok && amask != FULL) {
         emask = __ballot_sync(FULL, ahead);
         ne = __popc(emask);
@@ -407,7 +432,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
             ni = __popc(imask);
             maxj = (ni + ne - 1) / ne;
             if (!active) {
-                const uint32_t rank = __popc(imask & ((1u << lane) - 1u));
+                rank = __popc(imask & ((1u << lane) - 1u));
                 owner = nth_set_bit(emask, rank % ne);
                 offset = 2 + 2 * (rank / ne);
                 helper = true;
@@ -449,43 +474,46 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     float lv[2];
     uint32_t skb, fbb;
     lam.template eval<2>(qx, qy, qz, lv, skb, fbb);
-    int res = RAY_CONTINUE;
-    uint32_t kind = 0;   // 1: march, 2: normal, 3: hone
-    const float qdt0 = r.Qdt;
-    if (active) {
-        kind = sample_kind(r);
-        st.samples += 1;
-        st.skipped += skb & 1u;
-        st.fallback += fbb & 1u;
-        res = ray_advance(r, lv[0], prm, bracket_mode);
-        if (ahead && res == RAY_CONTINUE && still_ahead(r, kind, qdt0)) {
-            st.samples += 1;
-            st.skipped += (skb >> 1) & 1u;
-            st.fallback += (fbb >> 1) & 1u;
-            res = ray_advance(r, lv[1], prm, bracket_mode);
-        }
-    }
+    uint32_t bits = skb | (fbb << 2);
     if (ne) {
-        const bool own_elig = (emask >> lane) & 1u;
-        const uint32_t idx = __popc(emask & ((1u << lane) - 1u));
-        const uint32_t bits = skb | (fbb << 2);
-        for (uint32_t j = 1; j <= maxj; j++) {
-            const uint32_t rr = (j - 1) * ne + idx;
-            const bool have = own_elig && rr < ni;
-            const uint32_t src = have ? nth_set_bit(imask, rr) : lane;
-            const float l0 = __shfl_sync(FULL, lv[0], src);
-            const float l1 = __shfl_sync(FULL, lv[1], src);
-            const uint32_t b = __shfl_sync(FULL, bits, src);
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                if (have && res == RAY_CONTINUE && still_ahead(r, kind, qdt0)) {
-                    st.samples += 1;
-                    st.skipped += (b >> h) & 1u;
-                    st.fallback += (b >> (2 + h)) & 1u;
-                    st.spec_used += 1;
-                    res = ray_advance(r, h ? l1 : l0, prm, bracket_mode);
-                }
-            }
+        __syncwarp();   // the owners' reads of the previous round are done
+        if (helper) {
+            slot_l[warp][rank] = make_float2(lv[0], lv[1]);
+            slot_b[warp][rank] = bits;
+        }
+        __syncwarp();
+    }
+    int res = RAY_CONTINUE;
+    if (active) {
+        const uint32_t kind = sample_kind(r);   // 1: march, 2: normal, 3: hone
+        const float qdt0 = r.Qdt;
+        // this ray's helpers: ranks idx, idx + ne, ... below ni, two samples each
+        uint32_t idx = 0, nh = 0;
+        if (ne && ahead) {
+            idx = __popc(emask & ((1u << lane) - 1u));
+            nh = idx < ni ? (ni - idx + ne - 1) / ne : 0u;
+        }
+        float l0 = lv[0], l1 = lv[1];
+        // the own pair (its second sample only when known ahead), then the
+        // helpers' pairs in order while the ray continues in the phase they
+        // were taken for
+        for (uint32_t j = 0;; j++) {
+            st.samples += 1;
+            st.skipped += bits & 1u;
+            st.fallback += (bits >> 2) & 1u;
+            st.spec_used += j ? 1u : 0u;
+            res = ray_advance(r, l0, prm, bracket_mode);
+            if (res != RAY_CONTINUE || !ahead || !still_ahead(r, kind, qdt0)) break;
+            st.samples += 1;
+            st.skipped += (bits >> 1) & 1u;
+            st.fallback += (bits >> 3) & 1u;
+            st.spec_used += j ? 1u : 0u;
+            res = ray_advance(r, l1, prm, bracket_mode);
+            if (res != RAY_CONTINUE || j >= nh || !still_ahead(r, kind, qdt0)) break;
+            const float2 v = slot_l[warp][j * ne + idx];
+            l0 = v.x;
+            l1 = v.y;
+            bits = slot_b[warp][j * ne + idx];
         }
     }
     return res;
