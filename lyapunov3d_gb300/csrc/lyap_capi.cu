@@ -9,7 +9,9 @@
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "lyap_device.cuh"
@@ -38,6 +40,58 @@ int cuda_error(cudaError_t e, const char *what)
         e == cudaErrorInvalidDevice)
         code = LYAP_ERR_NO_DEVICE;
     return set_error(code, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+// Scratch and the host-buffer calls' device copies come from a stream-ordered
+// memory pool the library creates per device, which keeps up to
+// LYAP_POOL_KEEP_MB (default 1024) MiB of freed memory between calls.  The
+// device's default pool keeps nothing: every stream synchronisation hands
+// its memory back, and the next call maps it again (for lyap_render_host at
+// 1080p, 92 MB per call) while the GPU waits.  Without a pool of its own
+// (creation failed) the library allocates from the default pool.
+static uint64_t pool_keep_bytes()
+{
+    const char *v = getenv("LYAP_POOL_KEEP_MB");
+    if (v && *v) {
+        char *end = nullptr;
+        const unsigned long long mb = strtoull(v, &end, 10);
+        if (end && *end == '\0') return (uint64_t)mb << 20;
+    }
+    return (uint64_t)1024 << 20;
+}
+
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t s)
+{
+    static std::mutex mu;
+    static cudaMemPool_t pools[64];
+    static bool tried[64];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, s);
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!tried[dev]) {
+            tried[dev] = true;
+            cudaMemPoolProps props;
+            memset(&props, 0, sizeof(props));
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t created = nullptr;
+            if (cudaMemPoolCreate(&created, &props) == cudaSuccess) {
+                uint64_t keep = pool_keep_bytes();
+                cudaMemPoolSetAttribute(created, cudaMemPoolAttrReleaseThreshold, &keep);
+                pools[dev] = created;
+            } else {
+                (void)cudaGetLastError();   // not sticky: fall back to the default pool
+            }
+        }
+        pool = pools[dev];
+    }
+    if (!pool) return cudaMallocAsync(p, bytes, s);
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
 }
 
 static int check_params(const LyapParams *prm, const char *fn)
@@ -213,7 +267,7 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     const size_t list_off = (prop_end + 255) & ~(size_t)255;
     const size_t scratch = list_off + npix * sizeof(uint32_t);
     uint32_t *d_counter = nullptr;
-    cudaError_t e = cudaMallocAsync((void **)&d_counter, scratch, s);
+    cudaError_t e = scratch_alloc((void **)&d_counter, scratch, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: scratch allocation");
     e = cudaMemsetAsync(d_counter, 0, 2 * sizeof(uint32_t), s);
     job.list = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(d_counter) + list_off);
@@ -324,7 +378,7 @@ int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *s
     const size_t off_l = up(seq_b), off_r = off_l + up(light_b), off_p = off_r + up(rgba_b);
     const size_t total = off_p + up(pts_b);
     char *dev = nullptr;
-    cudaError_t e = cudaMallocAsync((void **)&dev, total, s);
+    cudaError_t e = scratch_alloc((void **)&dev, total, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render_host: device buffers");
     e = cudaMemcpyAsync(dev, seq, seq_b, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && light_b) e = cudaMemcpyAsync(dev + off_l, lights, light_b, cudaMemcpyHostToDevice, s);
@@ -367,7 +421,7 @@ int lyap_volume_host(float *out, uint32_t nx, uint32_t ny, uint32_t nz, const fl
     const size_t out_b = (size_t)nx * ny * nz * sizeof(float);
     const size_t seq_off = (out_b + 255) & ~(size_t)255;
     char *dev = nullptr;
-    cudaError_t e = cudaMallocAsync((void **)&dev, seq_off + seq_len * sizeof(int32_t), s);
+    cudaError_t e = scratch_alloc((void **)&dev, seq_off + seq_len * sizeof(int32_t), s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_volume_host: device buffers");
     e = cudaMemcpyAsync(dev + seq_off, seq, seq_len * sizeof(int32_t), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) {

@@ -44,6 +44,10 @@ cudaError_t launch_proposal(RenderJob &job, const LyapNet &net, float margin, ui
 // LyapRenderExt.proposal when the struct has the field, else null (lyap_capi.cu)
 const LyapNet *ext_proposal(const LyapRenderExt *ext);
 
+// stream-ordered scratch from the library's memory pool of the current
+// device (lyap_capi.cu); release with cudaFreeAsync
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t s);
+
 // error reporting (lyap_capi.cu)
 int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);

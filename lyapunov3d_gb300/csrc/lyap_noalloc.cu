@@ -4,14 +4,15 @@
 // Who needs it: callers that cannot or must not allocate device memory on
 // each call -- processes on devices or drivers without stream-ordered memory
 // pools (cudaDevAttrMemoryPoolsSupported = 0, e.g. some virtualised GPUs),
-// where lyap_render's cudaMallocAsync fails; applications that own every
+// where lyap_render's stream-ordered allocation fails; applications that own every
 // device allocation (a fixed memory budget or their own allocator) and
 // forbid libraries from allocating; render loops that must not risk an
 // allocation failing or blocking mid-frame when device memory runs out.
-// lyap_render allocates its one piece of scratch (the pixel queue's counter)
-// with cudaMallocAsync on every call; this variant takes that scratch from a
-// small array in the library's own device memory, which exists for as long
-// as the library is loaded.
+// lyap_render allocates its scratch (the pixel queue's counter and the list
+// of rays that meet the box) from a stream-ordered memory pool on every call;
+// this variant walks every pixel instead of a list and takes the counter
+// from a small array in the library's own device memory, which exists for as
+// long as the library is loaded.
 //
 // The scratch: g_render_noalloc_scratch, LYAP_NOALLOC_SCRATCH_BYTES (256)
 // bytes per device that loads the library, of which one call uses 4 bytes
