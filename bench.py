@@ -39,6 +39,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB of L2
+# DRAM bytes (read + write) of one launch of the chosen render on the default
+# frame (1920x1080, seed 1), from one ncu capture of that kernel on that frame
+# (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass, mean of 2 launches):
+# the outputs (40 B per pixel) stay in L2 at kernel end
+RENDER_DRAM_BYTES_FRAME1080 = 4575232 + 551296
 
 
 def parse_args():
@@ -393,6 +398,7 @@ def run_ours(args):
         cpu = {"value": r, "unit": "G iters/s", "cores": threads, "kind": "port",
                "sample": desc + f" ({t:.1f} s)"}
 
+    default_frame = (args.seed, wl.width, wl.height) == (1, 1920, 1080)
     if rank == 0:
         line = {
             "metric": "G logistic-iters/s (1080p Lyapunov raymarch frame)",
@@ -424,7 +430,10 @@ def run_ours(args):
             "surface": {"pixel_agreement": agree, "surface_pixel_agreement": surf_agree,
                         "lambda_at_hits_vs_plain": lam_diff},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "G iters/s",
-                         "frac": achieved / peak_fp32, "traffic": None,
+                         "frac": achieved / peak_fp32,
+                         "traffic": RENDER_DRAM_BYTES_FRAME1080 if default_frame else None,
+                         "traffic_unit": "DRAM bytes per launch (ncu capture of this frame)",
+                         "algorithmic_bytes": 40 * wl.width * wl.height,
                          "peak_source": "measured live: FFMA pipe-rate probe (lyap_pipe_probe) x (S+A)/(2S+4A) "
                                         "FP32 ops per iteration",
                          "probe_ffma_tops": probe["ffma"] / 1e12, "probe_lg2_tops": probe["lg2"] / 1e12,
