@@ -302,6 +302,38 @@ def run_ours(args):
     iters_frame = frame.iterations(chosen_st) // args.steps
     plain_iters_frame = frame.iterations(plain_st) // args.steps
 
+    # the reference's own entry point and launch shape: kernel_calc_render<<<(W/16, H/16), (16, 16)>>>
+    # (plain lambda; the grid covers H/16 whole rows of blocks, as the reference's launch does).
+    # Its iterations: the plain frame's per-pixel sample counts over the rows the grid covers.
+    gx, gy = wl.width // 16, wl.height // 16
+    dropin = None
+    if gx and gy:
+        cf = DeviceFrame(wl, device=dev, counts=True, stats=False)
+        cf.run(capi.VARIANT_PLAIN, stream=stream)
+        torch.cuda.synchronize()
+        dropin_iters = int(cf.counts()[:gy * 16].sum()) * (S + A)
+        del cf
+
+        def dropin_frame():
+            capi.kernel_calc_render((gx, gy), (16, 16), frame.d_rgba, frame.d_points, frame.cam, frame.prm,
+                                    frame.d_seq, frame.d_lights, len(frame.lights), stream=stream)
+        for _ in range(args.warmup):
+            dropin_frame()
+        torch.cuda.synchronize()
+        dts = []
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dropin_frame()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            dts.append(e0.elapsed_time(e1))
+        dms = max_over_ranks([statistics.mean(dts)], world, dev)[0]
+        dropin = {"kernel": f"kernel_calc_render<<<({gx}, {gy}), (16, 16)>>>", "rows": gy * 16,
+                  "value": dropin_iters / (dms * 1e-3) / 1e9 * world, "unit": "G iters/s", "ms_per_step": dms,
+                  "frame_ms": [round(t, 4) for t in dts]}
+
     # surface agreement and lambda difference between the chosen and the plain frame
     pts_c = frame.d_points.view(-1, 9).cpu().numpy()
     pts_p = plain_pts.view(-1, 9).cpu().numpy()
@@ -427,6 +459,8 @@ def run_ours(args):
                       "frames_per_s": world * args.steps / (t_plain * 1e-3),
                       "roofline_frac": plain_achieved / peak_plain},
             "speedup_vs_plain": value / plain_value,
+            "dropin_reference_launch": dropin,
+            "speedup_vs_dropin_reference_launch": value / dropin["value"] if dropin else None,
             "surface": {"pixel_agreement": agree, "surface_pixel_agreement": surf_agree,
                         "lambda_at_hits_vs_plain": lam_diff},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "G iters/s",
