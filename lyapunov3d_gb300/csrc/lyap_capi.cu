@@ -361,6 +361,41 @@ int lyap_volume(float *d_out, uint32_t nx, uint32_t ny, uint32_t nz, const float
     return LYAP_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The device address of a host output buffer the kernels can store into
+// directly, or null.  Page-locked host memory that the runtime has mapped into
+// the device's address space (allocated with cudaHostAlloc / cudaMallocHost,
+// or registered with cudaHostRegister) has one; the runtime reports it for the
+// first and the last byte of the range, which must lie in the same mapping.
+// On Grace-Blackwell the kernels' stores then reach host memory over
+// NVLink-C2C while the frame renders, and no download follows.  Pageable
+// memory, and anything the runtime cannot describe, takes the staging copy.
+void *mapped_host_view(void *host, size_t bytes)
+{
+    if (!host || bytes == 0) return nullptr;
+    cudaPointerAttributes a, b;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    if (cudaPointerGetAttributes(&b, static_cast<char *>(host) + bytes - 1) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (b.type != cudaMemoryTypeHost || !b.devicePointer ||
+        static_cast<char *>(b.devicePointer) - static_cast<char *>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a.devicePointer;
+}
+
+}  // namespace
+
+extern "C" {
+
 int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *seq, size_t seq_len,
                      const LyapLight *lights, uint32_t n_lights, RGBA *rgba, LyapPoint *points, uint32_t width,
                      uint32_t height, const LyapRenderExt *ext, void *stream)
@@ -373,7 +408,11 @@ int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *s
     const size_t npix = (size_t)width * height;
     const size_t seq_b = seq_len * sizeof(int32_t), light_b = (size_t)n_lights * sizeof(LyapLight);
     const size_t rgba_b = npix * sizeof(RGBA), pts_b = npix * sizeof(LyapPoint);
-    // one device block: [seq | lights | rgba | points], 256-byte aligned parts
+    // one device block: [seq | lights | rgba | points], 256-byte aligned parts.
+    // The outputs are always staged in device memory and downloaded in one
+    // copy each, page-locked or not: the render finishes pixels in scattered
+    // order, and storing them straight into mapped host memory over
+    // NVLink-C2C made the 1080p frame 1.8 ms slower than the 83 MB download.
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t off_l = up(seq_b), off_r = off_l + up(light_b), off_p = off_r + up(rgba_b);
     const size_t total = off_p + up(pts_b);
@@ -419,7 +458,9 @@ int lyap_volume_host(float *out, uint32_t nx, uint32_t ny, uint32_t nz, const fl
                          (unsigned long long)LYAP_MAX_VOXELS);
     cudaStream_t s = (cudaStream_t)stream;
     const size_t out_b = (size_t)nx * ny * nz * sizeof(float);
-    const size_t seq_off = (out_b + 255) & ~(size_t)255;
+    // an output in mapped page-locked host memory is written in place
+    float *out_direct = static_cast<float *>(mapped_host_view(out, out_b));
+    const size_t seq_off = out_direct ? 0 : (out_b + 255) & ~(size_t)255;
     char *dev = nullptr;
     cudaError_t e = scratch_alloc((void **)&dev, seq_off + seq_len * sizeof(int32_t), s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_volume_host: device buffers");
@@ -433,12 +474,13 @@ int lyap_volume_host(float *out, uint32_t nx, uint32_t ny, uint32_t nz, const fl
             x.size = sizeof(x);
         }
         if (!x.h_seq) x.h_seq = seq;
-        rc = lyap_volume((float *)dev, nx, ny, nz, lo, hi, prm, (const int32_t *)(dev + seq_off), seq_len, &x, stream);
+        rc = lyap_volume(out_direct ? out_direct : (float *)dev, nx, ny, nz, lo, hi, prm,
+                         (const int32_t *)(dev + seq_off), seq_len, &x, stream);
         if (rc) {
             cudaFreeAsync(dev, s);
             return rc;
         }
-        e = cudaMemcpyAsync(out, dev, out_b, cudaMemcpyDeviceToHost, s);
+        if (!out_direct) e = cudaMemcpyAsync(out, dev, out_b, cudaMemcpyDeviceToHost, s);
     }
     cudaError_t e2 = cudaFreeAsync(dev, s);
     cudaError_t e3 = cudaStreamSynchronize(s);
