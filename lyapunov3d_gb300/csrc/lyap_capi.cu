@@ -370,9 +370,10 @@ namespace {
 // the device's address space (allocated with cudaHostAlloc / cudaMallocHost,
 // or registered with cudaHostRegister) has one; the runtime reports it for the
 // first and the last byte of the range, which must lie in the same mapping.
-// On Grace-Blackwell the kernels' stores then reach host memory over
-// NVLink-C2C while the frame renders, and no download follows.  Pageable
-// memory, and anything the runtime cannot describe, takes the staging copy.
+// On Grace-Blackwell the volume sweep's coalesced streaming stores then reach
+// host memory over NVLink-C2C while it runs, and no download follows (512^3:
+// 18.0 ms per call instead of 20.8 with the staging copy).  Pageable memory,
+// and anything the runtime cannot describe, takes the staging copy.
 void *mapped_host_view(void *host, size_t bytes)
 {
     if (!host || bytes == 0) return nullptr;
