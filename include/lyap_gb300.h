@@ -378,7 +378,10 @@ int lyap_volume(float *d_out, uint32_t nx, uint32_t ny, uint32_t nz, const float
 /* Host-buffer forms of the two above (the reference front-ends' whole
  * round trip: upload, launch, download; lyap_interactive.cu:696-741,
  * lyap_calculate.cu:58-91).  seq / lights are host arrays, outputs are host
- * memory (points may be NULL); returns after the stream is synchronised. */
+ * memory (points may be NULL); returns after the stream is synchronised.
+ * lyap_volume_host writes a page-locked output (cudaHostAlloc,
+ * cudaHostRegister) in place from the kernel, without a staging copy;
+ * other outputs go through device memory. */
 int lyap_render_host(const LyapCam *cam, const LyapParams *prm, const int32_t *seq, size_t seq_len,
                      const LyapLight *lights, uint32_t n_lights, RGBA *rgba, LyapPoint *points,
                      uint32_t width, uint32_t height, const LyapRenderExt *ext, void *stream);
