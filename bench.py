@@ -423,6 +423,25 @@ def run_ours(args):
                   "write_gbs": n * 4 / (tp * 1e-3) / 1e9,
                   "write_frac_of_hbm": n * 4 / (tp * 1e-3) / 1e9 / peaks["hbm_gbs"]}
         del vol
+        if not args.no_e2e:
+            # end to end through lyap_volume_host into a page-locked host array (written in place)
+            pin = torch.empty(n * 4, dtype=torch.uint8, pin_memory=True)
+            out_h = pin.numpy().view(np.float32).reshape(args.volume, args.volume, args.volume)
+            vext = capi.LyapVolumeExt(variant=capi.VARIANT_PRODUCT, flags=capi.FLAG_NO_JIT if args.no_jit else 0)
+            capi.volume_host(args.volume, args.volume, args.volume, vw.params, capi.seq_parse(vw.seq), lo=vw.lo,
+                             hi=vw.hi, ext=vext, stream=stream, out=out_h)
+            hts = []
+            for i in range(3):
+                flush.fill_(float(i))
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                capi.volume_host(args.volume, args.volume, args.volume, vw.params, capi.seq_parse(vw.seq),
+                                 lo=vw.lo, hi=vw.hi, ext=vext, stream=stream, out=out_h)
+                hts.append(time.perf_counter() - t0)
+            volume["e2e"] = {"call": "lyap_volume_host (page-locked output, written in place)",
+                             "ms": 1e3 * statistics.mean(hts),
+                             "g_iters_s": vit / statistics.mean(hts) / 1e9, "d2h_bytes": n * 4}
+            del pin, out_h
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
