@@ -421,6 +421,11 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     __shared__ uint32_t slot_b[ROUND_WARPS][32];
     // can this ray's next positions be known before its current sample's lambda?
     const bool ahead = active && known_ahead(r, fixed_step);
+    // the ray's own second slot also takes its next hone step, assuming the
+    // sign of lambda does not flip (a coin toss while honing converges); the
+    // slot would otherwise evaluate a dummy, and the result is dropped when
+    // the step changed.  Helpers keep to the samples known_ahead allows.
+    const bool ahead_self = ahead || (active && r.phase == PH_HONE);
     uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
     bool helper = false;
     uint32_t owner = lane, offset = 0, rank = 0;
@@ -441,7 +446,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     }
     V3 Q0 = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
     V3 Q1 = v3(3.0f, 3.0f, 3.0f);
-    if (ahead) {
+    if (ahead_self) {
         bool v;
         Q1 = sample_ahead(r.P, r.V, r.dt, r.mag, r.QdV, r.phase, 1u, v);
     }
@@ -494,7 +499,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
             nh = idx < ni ? (ni - idx + ne - 1) / ne : 0u;
         }
         float l0 = lv[0], l1 = lv[1];
-        // the own pair (its second sample only when known ahead), then the
+        // the own pair (its second sample only when taken ahead), then the
         // helpers' pairs in order while the ray continues in the phase they
         // were taken for
         for (uint32_t j = 0;; j++) {
@@ -503,7 +508,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
             st.fallback += (bits >> 2) & 1u;
             st.spec_used += j ? 1u : 0u;
             res = ray_advance(r, l0, prm, bracket_mode);
-            if (res != RAY_CONTINUE || !ahead || !still_ahead(r, kind, qdt0)) break;
+            if (res != RAY_CONTINUE || !ahead_self || !still_ahead(r, kind, qdt0)) break;
             st.samples += 1;
             st.skipped += (bits >> 1) & 1u;
             st.fallback += (bits >> 3) & 1u;
