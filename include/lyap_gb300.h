@@ -460,8 +460,9 @@ int lyap_lambda_points(const float *d_xyz, size_t n, const LyapParams *prm, cons
 /* lyap_render without any device allocation.  It has no counterpart in the
  * reference (whose front-ends cudaMalloc everything up front).  For callers
  * that cannot allocate per call: devices or drivers without stream-ordered
- * memory pools (where lyap_render's cudaMallocAsync of its 4-byte queue
- * counter fails), applications that own all device memory and forbid
+ * memory pools (where lyap_render's stream-ordered allocation of its
+ * scratch -- the queue counter and the list of rays that meet the box --
+ * fails), applications that own all device memory and forbid
  * library allocations, loops that must not risk a failing or blocking
  * allocation mid-frame.  Same arguments and results as lyap_render; the
  * caller still passes all inputs and outputs.  The scratch is a static

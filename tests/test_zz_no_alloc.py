@@ -1,9 +1,9 @@
 """lyap_render_noalloc, the raymarch entry point that allocates nothing.
 
 Some callers cannot allocate device memory on every call: devices or drivers
-without stream-ordered memory pools (lyap_render's cudaMallocAsync of its
-queue counter fails there), applications that own all device memory, loops
-that must not risk an allocation failing mid-frame.  lyap_render_noalloc
+without stream-ordered memory pools (lyap_render's stream-ordered allocation
+of its queue counter and ray list fails there), applications that own all
+device memory, loops that must not risk an allocation failing mid-frame.  lyap_render_noalloc
 takes its scratch from a static device array instead.  This test calls it
 through the C ABI twice in a row (the second call must find the shared
 counter reset, not left at the first call's final count) and compares every
