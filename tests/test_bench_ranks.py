@@ -64,3 +64,26 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference"])
     bench.run_reference_arm(bench.parse_args())
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_line():
+    """--impl reference on a small frame prints one JSON line with the keys a
+    bench line carries: the metric and unit of the GPU arm, a cpu_baseline
+    describing the run, and an e2e object with no host-device traffic."""
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--width", "64",
+                        "--height", "36", "--steps", "1", "--warmup", "1"],
+                       capture_output=True, text=True, timeout=300, cwd=ROOT,
+                       env={k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")})
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert d["metric"] == "G logistic-iters/s (1080p Lyapunov raymarch frame)" and d["unit"] == "G iters/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 1
+    assert d["config"]["width"] == 64 and d["config"]["height"] == 36
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "G iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
