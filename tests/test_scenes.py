@@ -4,11 +4,17 @@ A seed names the same scene on every machine only if the generator and the
 scene construction never change, so they are pinned here: SplitMix64 against
 the published reference outputs for seed 1234567, and the benchmark frame,
 the 512^3 volume and the batched workload by their parameters and by the
-exact bytes of their cameras and lights (SHA-256 prefixes).
+exact bytes of their cameras and lights (SHA-256 prefixes).  The cameras are
+computed in double with the host libm's sin / cos before rounding to float,
+so the byte digests are pinned for the x86-64 build host; elsewhere only the
+parameters are checked.
 """
 import hashlib
+import platform
 
 from lyapunov3d_gb300 import scenes
+
+BYTES_PINNED = platform.machine() in ("x86_64", "AMD64")
 
 
 def _h(*parts):
@@ -32,8 +38,9 @@ def test_bench_frame_definition():
     assert (p.opaqueThreshold, p.chaosThreshold, p.nearThreshold, p.refine) == (-0.75, -0.5, -1.0, 32.0)
     assert (p.lMin, p.lMax) == (2.0, 4.0)
     assert len(wl.lights) == 1
-    assert _h(bytes(wl.cam)) == "6145a3e00ef72a7f"
-    assert _h(bytes(wl.lights[0])) == "f71170854ada571f"
+    if BYTES_PINNED:
+        assert _h(bytes(wl.cam)) == "6145a3e00ef72a7f"
+        assert _h(bytes(wl.lights[0])) == "f71170854ada571f"
 
 
 def test_volume_definition():
@@ -49,4 +56,5 @@ def test_batch_workload_definition():
     parts = []
     for w in b:
         parts += [w.seq.encode(), bytes(w.params), bytes(w.cam), f"{w.width}x{w.height}".encode()]
-    assert _h(*parts) == "f93bd7874221d60d"
+    if BYTES_PINNED:
+        assert _h(*parts) == "f93bd7874221d60d"
