@@ -164,35 +164,128 @@ def whole_job_rate(world, units_per_step, steps, seconds):
 
 
 # --------------------------------------------------------------- CPU arms
-def cpu_render_rate(wl, seconds, threads=0):
-    """The reference algorithm (oracle restatement of the reference's own
-    arithmetic, ORC_REF) on the host cores over seeded rows of the frame
-    until `seconds` of wall time; returns (G iters/s, description, threads)."""
-    from lyapunov3d_gb300 import capi
+def bench_config(wl, world):
+    """The workload as both arms print it (identical dicts: same frame, same
+    iteration counts, same timing policy)."""
+    return {"workload": wl.name, "width": wl.width, "height": wl.height, "steps_per_ray": int(wl.params.depth),
+            "step_method": int(wl.params.stepMethod), "settle": int(wl.params.settle),
+            "accum": int(wl.params.accum), "sequence": wl.seq, "box": [float(wl.params.lMin), float(wl.params.lMax)],
+            "l2": f"flushed between timed GPU frames ({L2_FLUSH_BYTES >> 20} MiB write)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def cpu_render_rate(wl, seconds, threads=0, fast_math=False, keep=False):
+    """The reference algorithm (the oracle's restatement of the reference's own
+    arithmetic, ORC_REF; camera, lights and sequence prepared by the oracle's
+    restatement of scene.cu too) on the host cores over seeded rows of the
+    frame until `seconds` of wall time.  fast_math: the same restatement built
+    -O3 -ffast-math (keeping IEEE infinities and NaN, which the ray setup needs).  Returns (G iters/s, description, threads, seconds, rows)
+    where rows = [(y, points, counts)] when `keep`, else []."""
     from oracle import ORC_REF, Oracle
-    orc = Oracle()
+    orc = Oracle(fast_math=fast_math)
     if threads:
         orc.set_threads(threads)
-    cam = capi.cam_recalculate(wl.cam, wl.width, wl.height, 1)
-    lights = capi.lights_recalculate(wl.lights)
-    seq = capi.seq_parse(wl.seq)
+    cam = orc.cam_recalculate(wl.cam, wl.width, wl.height, 1)
+    lights = orc.lights_recalculate(wl.lights)
+    rc, seq = orc.seq_parse(wl.seq)
+    if rc != 0:
+        raise ValueError(f"sequence {wl.seq!r}: oracle parse status {rc}")
     rows = np.random.default_rng(12345).permutation(wl.height)
-    iters, t, done = 0, 0.0, 0
+    iters, t, done, kept = 0, 0.0, 0, []
     per = wl.params.settle + wl.params.accum
     while done < len(rows) and t < seconds:
         y = int(rows[done])
         t0 = time.perf_counter()
-        _, _, cnt = orc.render(ORC_REF, wl.width, wl.height, cam, wl.params, seq, lights, y0=y, y1=y + 1)
+        _, pts, cnt = orc.render(ORC_REF, wl.width, wl.height, cam, wl.params, seq, lights, y0=y, y1=y + 1)
         t += time.perf_counter() - t0
         iters += int(cnt.sum()) * per
         done += 1
+        if keep:
+            kept.append((y, pts[0], cnt[0]))
+    build = "-O3 -ffast-math -fno-finite-math-only" if fast_math else "-O2"
     desc = (f"{done} of {wl.height} rows (seeded permutation) x {wl.width} px of the frame, reference arithmetic "
-            f"(double-promoted orbit, logf per step), {orc.threads()} OpenMP threads")
-    return iters / t / 1e9, desc, orc.threads(), t
+            f"(double-promoted orbit, logf per step), C restatement built {build}, {orc.threads()} OpenMP threads")
+    return iters / t / 1e9, desc, orc.threads(), t, kept
+
+
+def frame_parity(wl, rows, g_pts, g_cnt):
+    """The GPU frame against the reference's arithmetic on the CPU-baseline rows
+    (the oracle's ORC_REF, bit-exact to the reference's host build) and
+    against FP64 at the GPU frame's hit points in those rows.  Checker only;
+    runs after the timed region."""
+    from oracle import ORC_F64, ORC_REF, Oracle
+    orc = Oracle()
+    rc, seq = orc.seq_parse(wl.seq)
+    ys = np.array([y for y, _, _ in rows], dtype=np.int64)
+    r_pts = np.stack([p for _, p, _ in rows])
+    r_cnt = np.stack([c for _, _, c in rows])
+    gp, gc = g_pts[ys], g_cnt[ys]
+    dec = np.all(gc == r_cnt, axis=-1)
+    gh, rh = ~np.isnan(gp["a"]), ~np.isnan(r_pts["a"])
+    both = dec & gh & rh
+    same_p = both & np.all(gp["P"] == r_pts["P"], axis=-1)
+    gl, rl = gp["l"][both].astype(np.float64), r_pts["l"][both].astype(np.float64)
+    fin = np.isfinite(gl) & np.isfinite(rl)
+    dl = np.abs(gl[fin] - rl[fin])
+    # FP64 lambda at the GPU's hit points of those rows (float coordinates, the frame's d)
+    P = gp["P"][gh].astype(np.float64)
+    pts = np.concatenate([P, np.full((len(P), 1), float(wl.params.d))], axis=1)
+    l64 = orc.lyap4d(ORC_F64, pts, wl.params.settle, wl.params.accum, seq)
+    lref = orc.lyap4d(ORC_REF, pts, wl.params.settle, wl.params.accum, seq)
+    lgpu = gp["l"][gh].astype(np.float64)
+
+    def vs64(v):
+        ok = np.isfinite(v) & np.isfinite(l64)
+        d = np.abs(v[ok] - l64[ok])
+        return {"max_abs": float(d.max()) if d.size else 0.0, "mean_abs": float(d.mean()) if d.size else 0.0,
+                "median_abs": float(np.median(d)) if d.size else 0.0,
+                "p99_abs": float(np.quantile(d, 0.99)) if d.size else 0.0,
+                "nan_mismatch": int((np.isnan(v) != np.isnan(l64)).sum())}
+    return {
+        "rows": int(len(ys)), "pixels": int(dec.size),
+        "vs_reference_arithmetic": {
+            "oracle": "ORC_REF (restatement pinned bit-exact to the reference's host build)",
+            "decisions_agree": float(dec.mean()),
+            "hit_agreement": float((gh == rh).mean()),
+            "surface_pixel_agreement": float((gh & rh).sum() / max(1, (gh | rh).sum())),
+            "hit_points_identical_where_decisions_agree": float(same_p.sum() / max(1, both.sum())),
+            "lambda_at_hits_max_abs": float(dl.max()) if dl.size else 0.0,
+            "lambda_at_hits_mean_abs": float(dl.mean()) if dl.size else 0.0},
+        "vs_f64_at_gpu_hits": {"hits": int(gh.sum()), "chosen": vs64(lgpu), "reference_arithmetic": vs64(lref)},
+    }
+
+
+def volume_parity(vw, values, idx):
+    """lambda of the GPU volume at seeded voxels against FP64 and against the
+    reference's arithmetic (oracle), at the kernel's float32 voxel coordinates."""
+    from oracle import ORC_F64, ORC_REF, Oracle
+    orc = Oracle()
+    rc, seq = orc.seq_parse(vw.seq)
+    n = vw.n[0]
+    x, y, z = idx % n, (idx // n) % n, idx // (n * n)
+
+    def coord(lo, hi, i):
+        lo32, hi32 = np.float32(lo), np.float32(hi)
+        return lo32 + ((hi32 - lo32) * i.astype(np.float32)) / np.float32(n)
+    pts = np.stack([coord(vw.lo[0], vw.hi[0], x), coord(vw.lo[1], vw.hi[1], y), coord(vw.lo[2], vw.hi[2], z),
+                    np.full(len(idx), vw.params.d, dtype=np.float32)], axis=1).astype(np.float64)
+    l64 = orc.lyap4d(ORC_F64, pts, vw.params.settle, vw.params.accum, seq)
+    lref = orc.lyap4d(ORC_REF, pts, vw.params.settle, vw.params.accum, seq)
+    v = values.astype(np.float64)
+
+    def diff(a, b):
+        ok = np.isfinite(a) & np.isfinite(b)
+        d = np.abs(a[ok] - b[ok])
+        return {"max_abs": float(d.max()), "mean_abs": float(d.mean()), "median_abs": float(np.median(d)),
+                "p99_abs": float(np.quantile(d, 0.99)), "nan_mismatch": int((np.isnan(a) != np.isnan(b)).sum())}
+    return {"voxels": int(len(idx)), "chosen_vs_f64": diff(v, l64), "reference_arithmetic_vs_f64": diff(lref, l64),
+            "chosen_vs_reference_arithmetic": diff(v, lref)}
 
 
 def run_reference_arm(args):
-    """--impl reference: the reference algorithm on the host cores, same metric."""
+    """--impl reference: the reference algorithm on the host cores, same metric.
+    Nothing of the product library is loaded: scene preparation and the
+    render both run in the oracle's restatement of the reference."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
@@ -204,24 +297,21 @@ def run_reference_arm(args):
     rates, secs = [], 0.0
     desc, threads = "", 0
     for _ in range(args.steps):
-        r, desc, threads, t = cpu_render_rate(wl, per_step)
+        r, desc, threads, t, _ = cpu_render_rate(wl, per_step)
         rates.append(r)
         secs += t
     value = float(np.mean(rates))
-    frame_iters_est = None
     line = {
         "impl": "reference", "metric": "G logistic-iters/s (1080p Lyapunov raymarch frame)", "value": value,
         "unit": "G iters/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * secs / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
-        "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "steps_per_ray": 512,
-                   "settle": wl.params.settle, "accum": wl.params.accum, "sequence": wl.seq, "box": [2.0, 4.0]},
+        "config": bench_config(wl, world),
         "cpu_baseline": {"value": value, "unit": "G iters/s", "cores": threads, "kind": "port",
                          "sample": f"per step: {desc}"},
         "e2e": {"value": value, "unit": "G iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "host cores only; the reference's GPU path needs its GL front-end and its sources are not on "
                 "this host, so its algorithm runs through the oracle's bit-exact restatement",
-        "frame_iters_est": frame_iters_est,
     }
     print(json.dumps(line), flush=True)
 
@@ -399,7 +489,7 @@ def run_ours(args):
             "tail_frac": (t_end - t_drain) / max(1, t_end - t_start)} if t_end > t_drain > t_start else None
 
     # secondary: the dense volume sweep (HBM write-out roofline)
-    volume = None
+    volume = vol_sample = None
     if args.volume > 0:
         vw = scenes.full_volume(args.volume, args.seed)
         vol = DeviceVolume(vw, device=dev)
@@ -422,6 +512,10 @@ def run_ours(args):
                   "product_g_iters_s": vit / (tp * 1e-3) / 1e9, "plain_g_iters_s": vit / (tq * 1e-3) / 1e9,
                   "write_gbs": n * 4 / (tp * 1e-3) / 1e9,
                   "write_frac_of_hbm": n * 4 / (tp * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+        vidx = np.random.default_rng(512).choice(n, 8192, replace=False).astype(np.int64)
+        vol.run(capi.VARIANT_PRODUCT, stream=stream, jit=jit)
+        torch.cuda.synchronize()
+        vol_sample = (vw, vol.d_out[torch.from_numpy(vidx).to(dev)].cpu().numpy(), vidx)
         del vol
         if not args.no_e2e:
             # end to end through lyap_volume_host into a page-locked host array (written in place)
@@ -443,11 +537,21 @@ def run_ours(args):
                              "g_iters_s": vit / statistics.mean(hts) / 1e9, "d2h_bytes": n * 4}
             del pin, out_h
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        r, desc, threads, t = cpu_render_rate(wl, args.cpu_seconds)
+        r, desc, threads, t, kept = cpu_render_rate(wl, args.cpu_seconds, keep=True)
+        rf, descf, _, tf, _ = cpu_render_rate(wl, args.cpu_seconds / 2, fast_math=True)
         cpu = {"value": r, "unit": "G iters/s", "cores": threads, "kind": "port",
-               "sample": desc + f" ({t:.1f} s)"}
+               "sample": desc + f" ({t:.1f} s)",
+               "fast_math": {"value": rf, "unit": "G iters/s", "sample": descf + f" ({tf:.1f} s)"}}
+        # the checker, after the timed region: the CPU rows against the chosen frame
+        pf = DeviceFrame(wl, device=dev, counts=True, stats=False)
+        pf.run(capi.VARIANT_PRODUCT, stream=stream, jit=jit)
+        torch.cuda.synchronize()
+        parity = {"frame": frame_parity(wl, kept, pf.points(), pf.counts())}
+        del pf
+        if vol_sample is not None:
+            parity["volume"] = volume_parity(*vol_sample)
 
     default_frame = (args.seed, wl.width, wl.height) == (1, 1920, 1080)
     if rank == 0:
@@ -456,11 +560,8 @@ def run_ours(args):
             "value": value, "unit": "G iters/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_chosen / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene)",
-            "config": {"workload": wl.name, "width": wl.width, "height": wl.height, "steps_per_ray": 512,
-                       "step_method": 1, "settle": S, "accum": A, "sequence": wl.seq, "box": [2.0, 4.0],
-                       "variant": "product (renormalised FP32 product, one log2 per sample)",
-                       "l2": f"flushed between timed frames ({L2_FLUSH_BYTES >> 20} MiB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "config": bench_config(wl, world),
+            "form": "product (renormalised FP32 product, one log2 per sample), kernel specialised for the sequence",
             "frames_per_s": world * args.steps / (t_chosen * 1e-3),
             "frame_ms": [round(t, 4) for t in chosen_times],
             "iters_per_frame": iters_frame,
@@ -494,6 +595,7 @@ def run_ours(args):
             "e2e": e2e,
             "volume": volume,
             "cpu_baseline": cpu,
+            "parity": parity,
             # per timed frame: ray_list (the pre-pass) and render_persistent
             "gpu_launches": 2 * args.steps,
             "jit": capi.jit_info()[1].split("\n")[0] if jit else "off",

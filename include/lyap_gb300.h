@@ -464,16 +464,22 @@ int lyap_lambda_points(const float *d_xyz, size_t n, const LyapParams *prm, cons
  * scratch -- the queue counter and the list of rays that meet the box --
  * fails), applications that own all device memory and forbid
  * library allocations, loops that must not risk a failing or blocking
- * allocation mid-frame.  Same arguments and results as lyap_render; the
- * caller still passes all inputs and outputs.  The scratch is a static
+ * allocation mid-frame.  Same arguments and the same images as lyap_render
+ * with the precompiled kernels: it always launches those (it ignores
+ * ext->h_seq, and LYAP_FLAG_REQUIRE_JIT returns LYAP_ERR_INVALID_ARG), and it
+ * refuses the learned proposal and LYAP_FLAG_BISECT_F64, which need
+ * per-pixel scratch.  The caller still passes all inputs and outputs.  The
+ * scratch is a static
  * device array of LYAP_NOALLOC_SCRATCH_BYTES per device (held until the
  * library is unloaded), of which a call uses 4 bytes, zeroed on `stream`
  * before the launch; images are limited to LYAP_MAX_PIXELS (larger sizes
  * return LYAP_ERR_INVALID_ARG).  All calls share that array: calls whose
  * work overlaps on the GPU race and corrupt each other's images, so
  * serialise them.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture. */
+ * address (cudaGetSymbolAddress) with that device current and keeps it for
+ * the life of the process; make that first call before any stream capture,
+ * and do not call this entry point on a device after cudaDeviceReset there
+ * (the kept address then belongs to the destroyed context). */
 #define LYAP_NOALLOC_SCRATCH_BYTES 256
 int lyap_render_noalloc(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq, size_t seq_len,
                         const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,

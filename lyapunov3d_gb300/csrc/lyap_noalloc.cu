@@ -25,7 +25,13 @@
 // Set-up: host code cannot use the array's name as a device address (on the
 // host it names a stand-in object), so the first call on each device asks
 // the runtime for the address with cudaGetSymbolAddress while that device is
-// current and caches it.  Make that first call before any stream capture.
+// current and caches it for the life of the process (a cudaDeviceReset
+// destroys the context it belongs to: do not call this after one).  Make
+// that first call before any stream capture.
+//
+// Kernels: always the precompiled ones.  The run-time specialised kernels
+// are loaded into the context with cudaLibraryLoadData, which allocates, so
+// ext->h_seq is ignored here and LYAP_FLAG_REQUIRE_JIT is refused.
 // Nothing here calls cudaMalloc, cudaFree or any allocating routine.
 #include <cuda_runtime.h>
 
@@ -80,6 +86,10 @@ extern "C" int lyap_render_noalloc(const LyapCam *cam, const LyapParams *prm, co
     if (ext_proposal(ext))
         return set_error(LYAP_ERR_INVALID_ARG, "lyap_render_noalloc: the learned proposal needs scratch memory; "
                                                "use lyap_render");
+    if (ext && (ext->flags & LYAP_FLAG_REQUIRE_JIT))
+        return set_error(LYAP_ERR_INVALID_ARG, "lyap_render_noalloc: always runs the precompiled kernels "
+                                               "(loading a specialised kernel allocates); drop LYAP_FLAG_REQUIRE_JIT "
+                                               "or use lyap_render");
     if (ext && (ext->flags & LYAP_FLAG_BISECT_F64))
         return set_error(LYAP_ERR_INVALID_ARG,
                          "lyap_render_noalloc: LYAP_FLAG_BISECT_F64 needs per-pixel scratch; use lyap_render");

@@ -23,17 +23,22 @@ from lyapunov3d_gb300.types import (LyapCam, LyapCamD, LyapLight, LyapLightD, Ly
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liblyap_oracle.so")
+# the same restatement built -O3 -ffast-math: a second CPU-baseline build
+# (timing only; fast-math reorders the arithmetic, so it is not the pin)
+ORACLE_FASTMATH_SO = os.path.join(HERE, "_build", "liblyap_oracle_fastmath.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
 ORC_REF, ORC_PLAIN, ORC_PRODUCT, ORC_F64 = 0, 1, 2, -1
 ORC_HONE_CAP = 256
 
 
-def build_oracle(force=False):
-    """Compile oracle/_build/liblyap_oracle.so with make (gcc)."""
-    if force or not os.path.exists(ORACLE_SO):
+def build_oracle(force=False, fast_math=False):
+    """Compile oracle/_build/liblyap_oracle.so (and its -O3 -ffast-math twin)
+    with make (gcc); returns the path of the one asked for."""
+    path = ORACLE_FASTMATH_SO if fast_math else ORACLE_SO
+    if force or not os.path.exists(path):
         subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    return ORACLE_SO
+    return path
 
 
 def _ptr(a):
@@ -50,8 +55,8 @@ def _seq_array(seq):
 class Oracle:
     """The C restatement.  All array results are numpy arrays."""
 
-    def __init__(self, path=None):
-        path = path or build_oracle()
+    def __init__(self, path=None, fast_math=False):
+        path = path or build_oracle(fast_math=fast_math)
         L = ctypes.CDLL(path)
         self.lib = L
         L.orc_seq_parse.argtypes = [c_char_p, POINTER(c_int32), c_size_t, POINTER(c_size_t)]

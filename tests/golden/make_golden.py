@@ -2,8 +2,8 @@
 """Regenerate the golden fixtures from the reference's OWN code.
 
 Runs `make -C oracle ref` (the reference's kernel.cu / scene.cu / params.cu
-compiled as host C++ from the reference checkout, default /root/reference,
-override with LYAP_REF=...) and records what that build computes for seeded
+compiled as host C++ from the reference checkout: LYAP_REF=..., else a
+checkout named `reference` beside this repository) and records what that build computes for seeded
 inputs.  The fixtures pin the oracle restatement (tests/test_oracle_golden.py)
 and are compared with the CUDA path on the GPU (tests/test_gpu_parity.py).
 
@@ -51,7 +51,9 @@ def b(s):
 
 
 def main():
-    ref_dir = os.environ.get("LYAP_REF", "/root/reference")
+    ref_dir = os.environ.get("LYAP_REF") or os.path.join(os.path.dirname(ROOT), "reference")
+    if not os.path.isfile(os.path.join(ref_dir, "kernel.cu")):
+        sys.exit(f"make_golden: no reference checkout at {ref_dir} (set LYAP_REF=<checkout>)")
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref_dir}"], check=True)
     R32, R64 = Reference("f32"), Reference("f64")
     out = {}

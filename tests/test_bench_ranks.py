@@ -72,14 +72,24 @@ def test_reference_arm_json_line():
     describing the run, and an e2e object with no host-device traffic."""
     import json
     import subprocess
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--width", "64",
-                        "--height", "36", "--steps", "1", "--warmup", "1"],
-                       capture_output=True, text=True, timeout=300, cwd=ROOT,
+    # run bench.py as __main__, then report which of this repository's shared
+    # libraries the process loaded: the reference arm must not load the product's
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--width', '64', '--height', '36', "
+            "'--steps', '1', '--warmup', '1']; runpy.run_path('bench.py', run_name='__main__'); "
+            "print('LOADED', sorted({l.split()[-1].rsplit('/', 1)[-1] for l in open('/proc/self/maps') "
+            "if l.rstrip().endswith('.so') and 'lyap' in l}))")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=ROOT,
                        env={k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")})
     assert r.returncode == 0, r.stderr[-2000:]
+    loaded = [l for l in r.stdout.splitlines() if l.startswith("LOADED")]
+    assert loaded and "liblyap_gb300.so" not in loaded[0] and "liblyap_oracle.so" in loaded[0], loaded
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
+    # the same config dict as the GPU arm prints for this frame
+    import bench
+    from lyapunov3d_gb300 import scenes
+    assert d["config"] == json.loads(json.dumps(bench.bench_config(scenes.full_render(1, 64, 36), 1)))
     assert d["impl"] == "reference"
     assert d["metric"] == "G logistic-iters/s (1080p Lyapunov raymarch frame)" and d["unit"] == "G iters/s"
     assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] == 1

@@ -131,6 +131,21 @@ def test_render_ext_size_checked():
                                 a["points"], a["w"], a["h"], a["ext"], a["stream"]) == capi.LYAP_ERR_INVALID_ARG
 
 
+@pytest.mark.parametrize("flags,ext_kw,msg", [
+    (capi.FLAG_REQUIRE_JIT, {}, "precompiled"),
+    (capi.FLAG_BISECT_F64, {}, "LYAP_FLAG_BISECT_F64"),
+])
+def test_render_noalloc_refuses_what_needs_allocation(flags, ext_kw, msg):
+    """lyap_render_noalloc always runs the precompiled kernels and refuses the
+    modes that need scratch memory, before touching any device."""
+    ext = capi.LyapRenderExt(flags=flags, **ext_kw)
+    a, keep = _render_args(ext=ctypes.byref(ext))
+    rc = capi.lib.lyap_render_noalloc(a["cam"], a["prm"], a["seq"], a["seq_len"], a["lights"], a["n_lights"],
+                                      a["rgba"], a["points"], a["w"], a["h"], a["ext"], a["stream"])
+    assert rc == capi.LYAP_ERR_INVALID_ARG, capi.last_error()
+    assert capi.last_error().startswith("lyap_render_noalloc") and msg in capi.last_error()
+
+
 def test_volume_argument_errors():
     prm = LyapParams()
     L = capi.lib

@@ -198,9 +198,12 @@ def test_render_128_vs_oracle(dev, oracle, variant, mode):
 @pytest.mark.parametrize("case", ["preset64", "abc64", "inside48x32", "away32"])
 def test_render_golden_reference(dev, oracle, golden, case):
     """The reference's own renders (host build): the GPU's hit/miss agrees on
-    >= 99% of pixels (jittered cases carry lambda differences into the step
-    lengths); the oracle with the GPU's arithmetic reproduces the GPU's
-    decisions on >= 99.9%."""
+    >= 99.9% of pixels; without jitter the hit points are bit-identical to
+    the reference's on >= 99.9% of the pixels both hit, with lambda within
+    1e-4 there (jittered cases carry lambda differences of ~1e-6 into the
+    step lengths, so their points are compared statistically below); the
+    oracle with the GPU's arithmetic reproduces the GPU's decisions on
+    >= 99.9%."""
     meta, g = golden
     info = next(c for c in meta["render_cases"] if c["name"] == case)
     W, H = info["w"], info["h"]
@@ -220,7 +223,16 @@ def test_render_golden_reference(dev, oracle, golden, case):
     cnt = d_cnt.cpu().numpy().reshape(H, W, 3).astype(np.uint32)
     ref_pts = g[f"render_{case}_points"].view(POINT_DTYPE).reshape(H, W)
     hit_agree = (np.isnan(pts["a"]) == np.isnan(ref_pts["a"])).mean()
-    assert hit_agree >= 0.99, hit_agree
+    assert hit_agree >= 0.999, hit_agree
+    if prm.jitter == 0.0:
+        both = ~np.isnan(pts["a"]) & ~np.isnan(ref_pts["a"])
+        same = both & np.all(pts["P"] == ref_pts["P"], axis=-1)
+        assert same.sum() >= 0.999 * both.sum(), f"{same.sum()} of {both.sum()} hit points equal the reference's"
+        gl, rl = pts["l"][same].astype(np.float64), ref_pts["l"][same].astype(np.float64)
+        fin = np.isfinite(gl) & np.isfinite(rl)
+        assert np.array_equal(np.isnan(gl), np.isnan(rl))
+        if fin.any():
+            assert float(np.max(np.abs(gl[fin] - rl[fin]))) <= 1e-4
     r_rgba, r_pts, r_cnt = oracle.render(ORC_PLAIN, W, H, cam, prm, seq, lights)
     if prm.jitter == 0.0:
         _compare_frames(rgba, pts, cnt, r_rgba, r_pts, r_cnt)
@@ -229,7 +241,7 @@ def test_render_golden_reference(dev, oracle, golden, case):
         # later sample a little, so step counts may differ by one; hit / miss
         # must still agree and the hit points stay close
         gh, rh = ~np.isnan(pts["a"]), ~np.isnan(r_pts["a"])
-        assert (gh == rh).mean() >= 0.99
+        assert (gh == rh).mean() >= 0.999
         both = gh & rh
         dP = np.abs(pts["P"][both] - r_pts["P"][both]).max(axis=-1)
         assert np.median(dP) <= 1e-5 and np.quantile(dP, 0.9) <= 1e-2
