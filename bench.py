@@ -64,6 +64,8 @@ def parse_args():
                     help="--report proposal: skip thresholds above the opaque threshold")
     ap.add_argument("--proposal-segment", type=int, default=8, help="--report proposal: samples per segment")
     ap.add_argument("--train-steps", type=int, default=8192, help="--report proposal: Adam steps")
+    ap.add_argument("--proposal-grid", type=int, default=0, help="--report proposal: grid cells per axis (0 = 128)")
+    ap.add_argument("--proposal-dilate", type=int, default=0, help="--report proposal: 1 = dilate the grid")
     ap.add_argument("--report", choices=["precision", "batch", "proposal"], default=None,
                     help="instead of the benchmark, print the precision form's error report or time the batch")
     ap.add_argument("--batch-scale", type=int, default=1, help="--report batch: divide every image side by this")
@@ -714,10 +716,11 @@ def run_proposal_report(args):
     """The learned proposal on the 1080p frame (scenes.full_render): the net
     trained on the GPU (2^20 plain-method lambda samples; its kernels'
     gradients are checked against the CPU oracle in tests/test_gpu_net.py),
-    then the product-form frame with
-    the proposal at each margin against the same frame without it (and with
-    an untrained net at the same margins): device time, lambda samples
-    evaluated, surface agreement (pixels hit in both / hit by the plain
+    its grid over the box built once (the minimum of the net at each cell's
+    corners), then the product-form frame with the proposal at each margin
+    against the same frame without it (and with an untrained net at the same
+    margins): device time, lambda samples evaluated, skipped positions,
+    rewound runs, surface agreement (pixels hit in both / hit by the exact
     march) and same-sample agreement (hit at the bit-identical point)."""
     import ctypes
     import torch
@@ -732,7 +735,15 @@ def run_proposal_report(args):
     untrained = capi.net_train(wl.params, seq, steps=1, seed=args.seed)
     frame = DeviceFrame(wl, device=dev, counts=False)
     stream = torch.cuda.current_stream(dev)
-    flush = torch.empty(128 << 20, dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    # the grid: built once per net (timed here on its own), then cached by the library
+    n = args.proposal_grid or capi.PROPOSAL_GRID_DEFAULT
+    d_grid = torch.empty(n ** 3, dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    capi.net_grid(net, n, args.proposal_dilate, d_grid, stream=stream)
+    torch.cuda.synchronize()
+    t_grid = time.perf_counter() - t0
 
     def timed(**kw):
         for _ in range(max(1, args.warmup)):
@@ -753,15 +764,16 @@ def run_proposal_report(args):
     ms0, st0, p0 = timed()
     hit0 = ~np.isnan(p0[:, 0])
     rows = []
-    for which, n in (("trained", net), ("untrained", untrained)):
+    for which, nt in (("trained", net), ("untrained", untrained)):
         for m in (float(x) for x in args.margins.split(",")):
-            ms, st, p1 = timed(proposal=ctypes.pointer(n), proposal_margin=m, proposal_segment=args.proposal_segment)
+            ms, st, p1 = timed(proposal=ctypes.pointer(nt), proposal_margin=m, proposal_segment=args.proposal_segment,
+                               proposal_grid=n, proposal_dilate=args.proposal_dilate)
             hit1 = ~np.isnan(p1[:, 0])
             same = hit0 & hit1 & (p0[:, :3].view(np.uint32) == p1[:, :3].view(np.uint32)).all(1)
             rows.append({"net": which, "margin": m, "ms": ms, "speedup": ms0 / ms,
                          "samples_evaluated_frac": float(st[capi.STAT_SAMPLES] / st0[capi.STAT_SAMPLES]),
-                         "samples_skipped": int(st[capi.STAT_PROPOSAL_SKIPPED]),
-                         "net_points": int(st[capi.STAT_PROPOSAL_POINTS]),
+                         "positions_skipped": int(st[capi.STAT_PROPOSAL_SKIPPED]),
+                         "runs_rewound": int(st[capi.STAT_PROPOSAL_REWOUND]),
                          "net_timeouts": int(st[capi.STAT_NET_TIMEOUTS]),
                          "surface_agreement": float(hit1.sum() / max(1, hit0.sum())),
                          "same_sample_agreement": float(same.sum() / max(1, hit0.sum())),
@@ -771,6 +783,8 @@ def run_proposal_report(args):
         "train": {"seconds": t_train, "steps": net.steps, "batch": net.batch, "samples": net.n_samples,
                   "train_mse": net.train_mse, "val_mse": net.val_mse,
                   "loss_first10": float(np.mean(loss[:10])), "loss_last100": float(np.mean(loss[-100:]))},
+        "grid": {"cells_per_axis": n, "dilate": args.proposal_dilate, "build_s": t_grid,
+                 "net_points": (n + 1) ** 3},
         "segment": args.proposal_segment,
         "without_proposal": {"ms": ms0, "samples": int(st0[capi.STAT_SAMPLES]), "hits": int(hit0.sum())},
         "with_proposal": rows}), flush=True)

@@ -218,7 +218,9 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_STAT_MAX_ROUNDS 12  /* render: most rounds of any warp (max)     */
 #define LYAP_STAT_PROPOSAL_SKIPPED 13 /* render: march samples the learned
                                           proposal skipped (not evaluated) */
-#define LYAP_STAT_PROPOSAL_POINTS 14  /* render: points the proposal net evaluated */
+#define LYAP_STAT_PROPOSAL_POINTS 14  /* render: points the proposal net evaluated
+                                          (grid corners, when this call built
+                                          the net's grid; 0 when it was cached) */
 #define LYAP_STAT_NET_TIMEOUTS 15     /* tensor-core waits that ran out; the
                                           tiles concerned skip nothing */
 /* render timing (%globaltimer, ns): START and DRAIN hold the bitwise NOT of
@@ -229,7 +231,11 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_STAT_T_START  16
 #define LYAP_STAT_T_DRAIN  17
 #define LYAP_STAT_T_END    18
-#define LYAP_STAT_COUNT    19
+#define LYAP_STAT_PROPOSAL_REWOUND 19 /* render: confirming samples at or below the
+                                          proposal's threshold, each of which sent
+                                          its ray back to the start of the skipped
+                                          run (evaluated, then discarded) */
+#define LYAP_STAT_COUNT    20
 
 /* LyapRenderExt / LyapVolumeExt flags.  Given the host copy of the sequence
  * (h_seq), the library compiles the kernels for that sequence at run time
@@ -266,19 +272,28 @@ typedef struct {
     uint32_t bisect_halvings;    /* LYAP_FLAG_BISECT_F64: halvings (0 = 20) */
     uint32_t pad_;
     /* learned proposal (no reference counterpart): with a trained net
-     * (lyap_net_train), the march skips every segment of proposal_segment
-     * samples whose predicted lambda is >= opaqueThreshold + proposal_margin
-     * (with proposal_dilate, the neighbouring segments' predictions too).
-     * Every evaluated sample, hence every hit, is exact; a skipped segment
-     * adds nothing to the point's a and c sums.  Needs jitter 0 and
-     * nearMultiplier 1.  Callers built against the shorter struct (size =
-     * offsetof(LyapRenderExt, proposal)) keep working. */
+     * (lyap_net_train), the library evaluates the net once at the corners
+     * of a proposal_grid^3 grid over the net's box and keeps, per cell, the
+     * minimum (with proposal_dilate, the minimum over the 27 cells around);
+     * the grid is cached per device and net, so only the first call with a
+     * net pays for it (and synchronises its stream once).  The march then
+     * skips march positions whose cell holds a value >=
+     * opaqueThreshold + proposal_margin, at most proposal_segment - 1 in a
+     * row, and evaluates the position after every such run exactly: at or
+     * below that threshold the ray goes back to the run's first position and
+     * evaluates every position up to it.  So every hit is exact, and a
+     * surface is missed only where it enters and leaves the ray within one
+     * run the net called empty.  Skipped positions add nothing to the point's
+     * a and c sums.  Needs jitter 0 and nearMultiplier 1.  Callers built
+     * against the shorter struct (size = offsetof(LyapRenderExt, proposal))
+     * keep working. */
     const struct LyapNet *proposal; /* host struct, or NULL */
-    float proposal_margin;
-    uint32_t proposal_segment;   /* march samples per segment, 1..64 (0 = 8) */
+    float proposal_margin;       /* >= 0 */
+    uint32_t proposal_segment;   /* longest skipped run + 1, 1..64 (0 = 8) */
     uint32_t proposal_dilate;    /* 0 or 1 */
-    uint32_t pad2_;
+    uint32_t proposal_grid;      /* cells per axis, 2..512 (0 = LYAP_PROPOSAL_GRID_DEFAULT) */
 } LyapRenderExt;
+#define LYAP_PROPOSAL_GRID_DEFAULT 128u
 
 typedef struct {
     uint32_t size;               /* = sizeof(LyapVolumeExt) */
@@ -554,6 +569,13 @@ int lyap_output_name(char *buf, size_t cap, const char *kind, long stamp, uint32
  * Deterministic for a given seed.  Returns after the stream is synchronised. */
 int lyap_net_train(const LyapParams *prm, const int32_t *seq, size_t seq_len, const LyapNetTrainOptions *opt,
                    LyapNet *net, void *stream);
+/* The learned proposal's grid as lyap_render reads it: n^3 cells (x
+ * fastest) over the net's box, each the minimum of the net at the cell's 8
+ * corners (a NaN corner gives -inf), with dilate the minimum over the 27
+ * cells around it, into d_out[n^3] (device).  n = 0 takes
+ * LYAP_PROPOSAL_GRID_DEFAULT; 2..512.  Builds the grid on `stream` and caches
+ * it (as lyap_render does) if it is not cached yet. */
+int lyap_net_grid(const LyapNet *net, uint32_t n, uint32_t dilate, float *d_out, void *stream);
 /* The net at n points (d_xyz: 3 floats per point, device) into d_out[n]
  * (device), on the tensor cores.  Asynchronous. */
 int lyap_net_eval(const LyapNet *net, const float *d_xyz, size_t n, float *d_out, void *stream);

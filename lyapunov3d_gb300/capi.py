@@ -42,8 +42,13 @@ MAX_LIGHTS = 16
 
 (STAT_SAMPLES, STAT_SKIPPED, STAT_MARCH, STAT_HONE, STAT_NORMAL, STAT_HITS, STAT_RAYS, STAT_FALLBACK, STAT_SPEC,
  STAT_SPEC_USED, STAT_ROUNDS, STAT_LANE_ROUNDS, STAT_MAX_ROUNDS, STAT_PROPOSAL_SKIPPED, STAT_PROPOSAL_POINTS,
- STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END) = range(19)
-STAT_COUNT = 19
+ STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END, STAT_PROPOSAL_REWOUND) = range(20)
+STAT_COUNT = 20
+PROPOSAL_GRID_DEFAULT = 128
+# the proposal margin the library's users are pointed to: the smallest of the
+# measured margins at which the 1080p bench frame keeps >= 99.9 % of its
+# surface pixels (bench.py --report proposal)
+PROPOSAL_MARGIN_DEFAULT = 1.0
 
 NET_MAGIC = 0x4E50594C
 NET_VERSION = 1
@@ -87,7 +92,7 @@ class LyapRenderExt(ctypes.Structure):
                 ("d_counts", c_void_p), ("d_stats", c_void_p), ("blocks_per_sm", c_uint32),
                 ("threads_per_block", c_uint32), ("h_seq", c_void_p), ("bisect_halvings", c_uint32),
                 ("pad_", c_uint32), ("proposal", POINTER(LyapNet)), ("proposal_margin", c_float),
-                ("proposal_segment", c_uint32), ("proposal_dilate", c_uint32), ("pad2_", c_uint32)]
+                ("proposal_segment", c_uint32), ("proposal_dilate", c_uint32), ("proposal_grid", c_uint32)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -143,7 +148,7 @@ EXPORTED = ["lyap_abi_version", "lyap_version", "lyap_last_error_string", "lyap_
             "lyap_volume", "lyap_render_host", "lyap_volume_host", "lyap_kernel_calc_render",
             "lyap_kernel_calc_volume", "lyap_pipe_probe", "lyap_render_noalloc", "lyap_jit_info",
             "lyap_lambda_points", "lyap_batch_create", "lyap_batch_run", "lyap_batch_info", "lyap_batch_destroy",
-            "lyap_net_train", "lyap_net_eval", "lyap_net_grad", "lyap_net_save", "lyap_net_load",
+            "lyap_net_train", "lyap_net_eval", "lyap_net_grid", "lyap_net_grad", "lyap_net_save", "lyap_net_load",
             "lyap_params_init", "lyap_params_init_d", "lyap_ease_in_out_quart", "lyap_anim_camera",
             "lyap_anim_camera_d", "lyap_write_ppm", "lyap_write_points", "lyap_write_exps", "lyap_output_name",
             "lyap_cam_recalculate_d", "lyap_lights_recalculate_d", "lyap_render_d"]
@@ -182,6 +187,7 @@ def _load():
     L.lyap_batch_destroy.argtypes = [c_void_p]
     L.lyap_net_train.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
     L.lyap_net_eval.argtypes = [c_void_p, c_void_p, c_size_t, c_void_p, c_void_p]
+    L.lyap_net_grid.argtypes = [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p]
     L.lyap_net_grad.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p]
     L.lyap_net_save.argtypes = [c_void_p, c_char_p]
     L.lyap_net_load.argtypes = [c_void_p, c_char_p]
@@ -406,6 +412,11 @@ def net_train(prm, seq, stream=None, box_lo=None, box_hi=None, with_loss=False, 
     _check(lib.lyap_net_train(ctypes.byref(prm), _vp(seq), seq.size, ctypes.byref(o), ctypes.byref(net),
                               _stream(stream)))
     return (net, loss) if with_loss else net
+
+
+def net_grid(net, n, dilate, d_out, stream=None):
+    """lyap_net_grid: the proposal grid lyap_render reads (n^3 floats, x fastest) into d_out."""
+    _check(lib.lyap_net_grid(ctypes.byref(net), n, dilate, _vp(d_out), _stream(stream)))
 
 
 def net_eval(net, d_xyz, n, d_out, stream=None):

@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(128, 4) render_batch(const __grid_constant__ B
             slot_end = slots_per_chunk;
             continue;
         }
-        const int res = sample_round(r, active, amask, lam, prm, spec_ok, false, st);
+        const int res = sample_round<false>(r, active, amask, lam, prm, spec_ok, false, PropGrid{}, st);
         if (active && res != RAY_CONTINUE) {
             finish_pixel(J->rgba, J->points, J->counts, pix, r, res == RAY_HIT, cr.C, J->lights, J->n_lights,
                          J->light_model, st);

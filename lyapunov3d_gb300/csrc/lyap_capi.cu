@@ -139,8 +139,10 @@ static int check_ext_render(const LyapRenderExt *ext, const LyapParams *prm, con
         for (int k = 0; k < 3; k++)
             if (!(net->hi[k] > net->lo[k]))
                 return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal net has an empty box on axis %d", fn, k);
-        if (!std::isfinite(ext->proposal_margin))
-            return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal_margin is not finite", fn);
+        if (!std::isfinite(ext->proposal_margin) || ext->proposal_margin < 0.0f)
+            return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal_margin must be finite and >= 0", fn);
+        if (ext->proposal_grid == 1 || ext->proposal_grid > 512)
+            return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal_grid %u outside 2..512", fn, ext->proposal_grid);
         if (ext->proposal_segment > 64)
             return set_error(LYAP_ERR_INVALID_ARG, "%s: proposal_segment %u > 64", fn, ext->proposal_segment);
         if (ext->proposal_dilate > 1)
@@ -247,24 +249,34 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     RenderJob job = make_job(cam, prm, d_seq, seq_len, d_lights, n_lights, d_rgba, d_points, width, height, ext);
+    // the learned proposal's grid over the net's box: built on this stream on
+    // first use (then cached per device and net), read by the march
+    if (const LyapNet *net = ext_proposal(ext)) {
+        const uint32_t n = ext->proposal_grid ? ext->proposal_grid : LYAP_PROPOSAL_GRID_DEFAULT;
+        const uint32_t seg = ext->proposal_segment ? ext->proposal_segment : 8u;
+        const float *grid = nullptr;
+        cudaError_t ge = proposal_grid(*net, n, ext->proposal_dilate, &grid, ext->d_stats, s);
+        if (ge != cudaSuccess) return cuda_error(ge, "lyap_render: proposal grid");
+        job.prop.grid = grid;
+        job.prop.n = n;
+        job.prop.run = seg - 1;
+        for (int k = 0; k < 3; k++) {
+            job.prop.lo[k] = net->lo[k];
+            job.prop.scale[k] = (float)n / (net->hi[k] - net->lo[k]);
+        }
+        job.prop.tau = prm->opaqueThreshold + ext->proposal_margin;
+    }
     // scratch, stream-ordered so concurrent calls on different streams each
     // get their own: a 256-byte header (the queue's counter, the ray list's
     // length), the list of rays that meet the box (ray_list); with FP64
     // bisection also the per-pixel crossing brackets and the list of pixels
-    // that crossed (scratch of the two passes); with a learned proposal the
-    // net, the crossing rays and the per-pixel segment bits
+    // that crossed (scratch of the two passes)
     const bool bisect = ext && (ext->flags & LYAP_FLAG_BISECT_F64);
     const size_t npix = (size_t)width * height;
-    const LyapNet *net = ext_proposal(ext);
-    const uint32_t seg_len = net ? (ext->proposal_segment ? ext->proposal_segment : 8u) : 0u;
-    uint32_t words = 0;
-    if (net && proposal_segments(*prm, seg_len, &words) == 0) net = nullptr;
     const size_t bisect_bytes = bisect ? 256 + (((npix + 1) * sizeof(uint32_t) + 255) & ~(size_t)255) +
                                              npix * 2 * sizeof(float)
                                        : 256;
-    const size_t prop_off = (bisect_bytes + 255) & ~(size_t)255;
-    const size_t prop_end = net ? prop_off + proposal_scratch_bytes(npix, words) : bisect_bytes;
-    const size_t list_off = (prop_end + 255) & ~(size_t)255;
+    const size_t list_off = (bisect_bytes + 255) & ~(size_t)255;
     const size_t scratch = list_off + npix * sizeof(uint32_t);
     uint32_t *d_counter = nullptr;
     cudaError_t e = scratch_alloc((void **)&d_counter, scratch, s);
@@ -280,9 +292,6 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
         job.bracket = reinterpret_cast<float *>(base + 256 + (((npix + 1) * sizeof(uint32_t) + 255) & ~(size_t)255));
         e = cudaMemsetAsync(job.hits, 0, sizeof(uint32_t), s);
     }
-    if (e == cudaSuccess && net)
-        e = launch_proposal(job, *net, ext->proposal_margin, seg_len, ext->proposal_dilate,
-                            reinterpret_cast<char *>(d_counter) + prop_off, ext->d_stats, s);
     if (e == cudaSuccess) {
         const uint32_t variant = ext ? ext->variant : LYAP_VARIANT_PLAIN;
         const uint32_t flags = ext ? ext->flags : 0u;

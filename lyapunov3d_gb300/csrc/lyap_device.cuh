@@ -23,6 +23,7 @@
 #include <stdint.h>
 
 #include "lyap_gb300.h"
+#include "lyap_jobs.h"
 
 namespace lyapgb {
 
@@ -879,6 +880,14 @@ struct Ray {
     uint32_t phase, nm, nh, cap;
     uint32_t ns;     // march samples the learned proposal skipped (counted in nm, never evaluated)
     bool near, sign;
+    // learned proposal only (ray_advance<true>): the pending march sample
+    // confirms a run of `prun` skipped positions that began at (Ps, ts, tps);
+    // positions are evaluated exactly while nm < pnoskip; pgen counts the
+    // rewinds (samples taken ahead for this ray are stale once it changes);
+    // prej the samples a rewind discarded
+    V3 Ps;
+    float ts, tps;
+    uint32_t prun, pnoskip, pgen, prej;
 };
 
 struct CamRays {   // the per-frame camera quantities raymarch reads
@@ -895,6 +904,7 @@ __device__ __forceinline__ CamRays cam_rays(const LyapCam &cam)
 // ray misses the box [lMin, lMax]^3 (raymarch returns 1 before any sample).
 __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapParams &prm, uint32_t sx, uint32_t sy)
 {
+    r.prun = r.pnoskip = r.pgen = r.prej = 0;
     V3 V = (cam.S0 + cam.SDX * (float)sx) + cam.SDY * (float)sy;
     V = normalized(V);
     V = V / cam.M;
@@ -959,6 +969,89 @@ __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapP
     return true;
 }
 
+// ---------------------------------------------------- the learned proposal
+// Is the march position P in a cell whose lower bound of the net's lambda
+// is at least the skip threshold?  Positions outside the grid never are.
+__device__ __forceinline__ bool prop_skippable(const PropGrid &pg, V3 P)
+{
+    const float nf = (float)pg.n;
+    const float fx = (P.x - pg.lo[0]) * pg.scale[0];
+    const float fy = (P.y - pg.lo[1]) * pg.scale[1];
+    const float fz = (P.z - pg.lo[2]) * pg.scale[2];
+    if (!(fx >= 0.0f && fx < nf && fy >= 0.0f && fy < nf && fz >= 0.0f && fz < nf)) return false;
+    const uint32_t ix = (uint32_t)fx, iy = (uint32_t)fy, iz = (uint32_t)fz;   // each < n
+    return __ldg(pg.grid + ((size_t)iz * pg.n + iy) * pg.n + ix) >= pg.tau;
+}
+
+// After a march step (the ray at its next position P, index nm + 1): skip
+// the run of skippable positions that starts there -- at most pg.run, and
+// never the last position before t1 or the sample cap -- by taking exactly
+// the steps ray_advance takes after a sample above the threshold, so every
+// later position is bit-identical to the exact march's.  The ray then waits
+// at the position after the run, whose sample confirms it (ray_advance).
+// Counts: the skipped positions are in nm and ns.
+__device__ __forceinline__ void prop_form_run(Ray &r, const PropGrid &pg)
+{
+    if (r.nm < r.pnoskip) return;
+    uint32_t k = 0;
+    V3 Q = r.P;
+    float tq = r.t, tpq = r.tprev;
+    while (k < pg.run && r.nm + k + 1 < r.cap && prop_skippable(pg, Q)) {
+        const float tn = tq + r.dt;
+        if (tn > r.t1) break;   // Q is the last position in the box: it confirms
+        tpq = tq;
+        tq = tn;
+        Q = Q + r.V * r.dt;
+        k++;
+    }
+    if (k) {
+        r.Ps = r.P;
+        r.ts = r.t;
+        r.tps = r.tprev;
+        r.P = Q;
+        r.t = tq;
+        r.tprev = tpq;
+        r.nm += k;
+        r.ns += k;
+        r.prun = k;
+    }
+}
+
+// The march position `offset` evaluated samples after the pending one at P
+// (index nm + 1), assuming every sample until then is above the threshold
+// and confirms its run: the positions ray_advance<true> and prop_form_run
+// visit.  valid = false once the ray would have left the box or the cap.
+__device__ __forceinline__ V3 prop_march_ahead(V3 P, V3 V, float dt, float t, float t1, uint32_t nm, uint32_t cap,
+                                               uint32_t noskip, const PropGrid &pg, uint32_t offset, bool &valid)
+{
+    valid = true;
+    for (uint32_t j = 0; j < offset; j++) {
+        nm += 1;
+        if (nm >= cap) {
+            valid = false;
+            return P;
+        }
+        t = t + dt;
+        P = P + V * dt;
+        if (t > t1) {
+            valid = false;
+            return P;
+        }
+        if (nm >= noskip) {
+            uint32_t k = 0;
+            while (k < pg.run && nm + k + 1 < cap && prop_skippable(pg, P)) {
+                const float tn = t + dt;
+                if (tn > t1) break;
+                t = tn;
+                P = P + V * dt;
+                k++;
+            }
+            nm += k;
+        }
+    }
+    return P;
+}
+
 // Where the next lambda sample of this ray is taken.
 __device__ __forceinline__ V3 ray_sample_point(const Ray &r)
 {
@@ -982,8 +1075,16 @@ __device__ __forceinline__ V3 ray_sample_point(const Ray &r)
 enum : int { RAY_CONTINUE = 0, RAY_HIT = 1, RAY_MISS = 2, RAY_BRACKET = 3 };
 
 // Feed one lambda sample to the ray (kernel.cu:318-473); the ray either asks
-// for its next sample (RAY_CONTINUE) or ends.
-__device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &prm, bool bracket = false)
+// for its next sample (RAY_CONTINUE) or ends.  PROP: the learned proposal's
+// skipping (prop_form_run) after every march step, and the confirmation of
+// every skipped run by the sample after it: a confirming lambda at or below
+// pg.tau (the threshold the skip was made for) sends the ray back to the
+// run's first position, from where every position up to the confirming one
+// is evaluated exactly -- so a surface is lost only if it enters and leaves
+// the ray inside one run of positions the net called empty.
+template <bool PROP = false>
+__device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &prm, bool bracket = false,
+                                           const PropGrid *pg = nullptr)
 {
     const float opaque = prm.opaqueThreshold;
     bool to_normal = false;
@@ -1018,6 +1119,24 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
             }
         }
     } else {
+        if constexpr (PROP) {
+            if (r.prun) {
+                if (!(lam > pg->tau)) {
+                    // not clearly empty (NaN included): rewind the run
+                    r.P = r.Ps;
+                    r.t = r.ts;
+                    r.tprev = r.tps;
+                    r.nm -= r.prun;
+                    r.ns -= r.prun;
+                    r.pnoskip = r.nm + r.prun + 1;
+                    r.prun = 0;
+                    r.pgen += 1;
+                    r.prej += 1;
+                    return RAY_CONTINUE;
+                }
+                r.prun = 0;   // confirmed: the sample is the march sample at this position
+            }
+        }
         r.nm += 1;
         r.l = lam;
         if (r.phase == PH_MARCH) {
@@ -1048,6 +1167,7 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
             r.P = r.P + r.V * step;
             if (r.t > r.t1) return RAY_MISS;
             r.phase = PH_MARCH;
+            if constexpr (PROP) prop_form_run(r, *pg);
             return RAY_CONTINUE;
         }
         if (r.t > r.t1) return RAY_MISS;

@@ -34,13 +34,12 @@ RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_s
                    const LyapLight *d_lights, uint32_t n_lights, RGBA *d_rgba, LyapPoint *d_points,
                    uint32_t width, uint32_t height, const LyapRenderExt *ext);
 
-// the learned proposal (lyap_net.cu): march segments covered for a seg_len
-// (0 = none), the scratch the proposal pass needs, and the pass itself, which
-// fills job.skip*
-uint32_t proposal_segments(const LyapParams &prm, uint32_t seg_len, uint32_t *words);
-size_t proposal_scratch_bytes(size_t npix, uint32_t words);
-cudaError_t launch_proposal(RenderJob &job, const LyapNet &net, float margin, uint32_t seg_len, uint32_t dilate,
-                            void *scratch, unsigned long long *stats, cudaStream_t stream);
+// the learned proposal (lyap_net.cu): the net's grid of n^3 cells over its
+// box (the minimum of the net at each cell's corners; with dilate the
+// minimum over the 27 cells around), built on `stream` on first use and
+// cached per device, net hash, n and dilation for the life of the process
+cudaError_t proposal_grid(const LyapNet &net, uint32_t n, uint32_t dilate, const float **grid,
+                          unsigned long long *stats, cudaStream_t stream);
 // LyapRenderExt.proposal when the struct has the field, else null (lyap_capi.cu)
 const LyapNet *ext_proposal(const LyapRenderExt *ext);
 

@@ -87,6 +87,9 @@ struct Nvrtc {
     }
 };
 
+// One compiled specialisation: the render and volume kernels of both lambda
+// forms, or (a proposal entry, compiled on the first render with a learned
+// proposal) the render kernels with the proposal, render_persistent<Lam, true>.
 struct Entry {
     bool ok = false;
     std::string error;
@@ -174,11 +177,15 @@ std::string lam_type(const Spec &s, int mode)
            hex64(s.a1) + ">>";
 }
 
-void compile_entry(Entry &e, const Spec &s)
+void compile_entry(Entry &e, const Spec &s, bool prop)
 {
     Nvrtc &N = g_nvrtc;
     std::vector<std::string> names;
     for (int mode = 0; mode < 2; mode++) {
+        if (prop) {
+            names.push_back("&lyapgb::render_persistent<" + lam_type(s, mode) + ", true>");
+            continue;
+        }
         names.push_back("&lyapgb::render_persistent<" + lam_type(s, mode) + ">");
         names.push_back("&lyapgb::volume_sweep<" + lam_type(s, mode) + ", " + std::to_string(LYAP_JIT_VOLUME_K) +
                         ">");
@@ -233,8 +240,10 @@ void compile_entry(Entry &e, const Spec &s)
         return;
     }
     for (int mode = 0; mode < 2; mode++) {
-        ce = cudaLibraryGetKernel(&e.render[mode], e.lib, lowered[2 * mode].c_str());
-        if (ce == cudaSuccess) ce = cudaLibraryGetKernel(&e.volume[mode], e.lib, lowered[2 * mode + 1].c_str());
+        const size_t per = prop ? 1 : 2;
+        ce = cudaLibraryGetKernel(&e.render[mode], e.lib, lowered[per * mode].c_str());
+        if (ce == cudaSuccess && !prop)
+            ce = cudaLibraryGetKernel(&e.volume[mode], e.lib, lowered[per * mode + 1].c_str());
         if (ce != cudaSuccess) {
             e.error = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(ce);
             return;
@@ -245,7 +254,7 @@ void compile_entry(Entry &e, const Spec &s)
 
 // The cached specialisation for this sequence, compiling it on first use.
 // Returns null (with *why set) when the path is unavailable.
-Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string *why)
+Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string *why, bool prop = false)
 {
     if (jit_disabled_by_env()) {
         *why = "disabled by LYAP_JIT=0";
@@ -265,7 +274,7 @@ Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string 
         return nullptr;
     }
     const Spec s = make_spec(h_seq, L, settle);
-    const std::string key = lam_type(s, 9);
+    const std::string key = lam_type(s, 9) + (prop ? "|proposal" : "");
     std::lock_guard<std::mutex> lock(g_mu);
     if (g_nvrtc_state == 0) g_nvrtc_state = g_nvrtc.load() ? 1 : -1;
     if (g_nvrtc_state < 0) {
@@ -275,7 +284,7 @@ Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string 
     auto it = g_cache.find(key);
     if (it == g_cache.end()) {
         std::unique_ptr<Entry> e(new Entry());
-        compile_entry(*e, s);
+        compile_entry(*e, s, prop);
         g_compiles++;
         it = g_cache.emplace(key, std::move(e)).first;
     }
@@ -292,7 +301,7 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
                       unsigned long long *d_stats, uint32_t blocks_per_sm, uint32_t threads, cudaStream_t stream,
                       cudaError_t *launch_err, std::string *why)
 {
-    Entry *e = get_entry(h_seq, job.seq_period, job.prm.settle, why);
+    Entry *e = get_entry(h_seq, job.seq_period, job.prm.settle, why, job.prop.grid != nullptr);
     if (!e) return 0;
     const int sms = device_sm_count();
     if (sms <= 0) {

@@ -7,6 +7,19 @@
 
 namespace lyapgb {
 
+// The learned proposal as the march reads it: a lower bound of the net's
+// lambda per cell of an n^3 grid over the net's box.  A march position whose
+// cell holds a value >= tau (opaque threshold + margin) may be skipped, at
+// most `run` positions in a row; the sample after every run is evaluated
+// exactly and confirms it (prop_form_run and ray_advance, lyap_device.cuh).
+struct PropGrid {
+    const float *grid;           // device, n^3 floats, x fastest; null = no proposal
+    uint32_t n;                  // cells per axis
+    uint32_t run;                // longest run of skipped positions (segment length - 1)
+    float lo[3], scale[3];       // cell coordinate = (P - lo) * scale
+    float tau;                   // skip / confirm threshold
+};
+
 // One frame to render: everything kernel_calc_render receives (kernel.cu:500)
 // plus the image size, the light model and optional outputs.
 struct RenderJob {
@@ -26,14 +39,8 @@ struct RenderJob {
     // it; a second pass bisects it in double (lyap_precise.cu)
     float *bracket;              // device, 2 per pixel: t of the last sample above, first at/below
     uint32_t *hits;              // device, [0] = count, then the pixel indices that crossed
-    // learned proposal: per pixel skip_words words of bits, bit j set when the
-    // net predicts lambda above the skip threshold for march segment j
-    // (samples j*seg_len .. j*seg_len + seg_len - 1); null = no proposal
-    const uint32_t *skip;
-    uint32_t skip_words;         // words per pixel
-    uint32_t skip_segments;      // segments covered by the bits (later samples are always evaluated)
-    uint32_t seg_len;            // march samples per segment
-    uint32_t skip_dilate;        // 1: a segment is skipped only if its neighbours' bits are set too
+    // learned proposal (render_persistent<Lam, true> only; grid null = none)
+    PropGrid prop;
     // the rays that meet the box, listed by ray_list (null: the queue runs
     // over every pixel); the render's queue hands out list[i]
     const uint32_t *list;

@@ -149,6 +149,7 @@ struct LaneStats {
     uint32_t samples, skipped, march, hone, normal, hits, rays, fallback, spec, spec_used;
     uint32_t rounds, lane_rounds;   // per warp, kept by every lane alike
     uint32_t prop_skip;             // march samples skipped on the learned proposal's word
+    uint32_t prop_rej;              // samples a rewind of the proposal discarded
 };
 
 // position of the n-th (0-based) set bit of mask; mask has more than n bits
@@ -217,6 +218,7 @@ __device__ __forceinline__ void finish_pixel(RGBA *rgba, LyapPoint *points, uint
     }
     st.march += r.nm - r.ns;
     st.prop_skip += r.ns;
+    st.prop_rej += r.prej;
     st.hone += r.nh;
     st.normal += hit ? 6u : 0u;
     st.hits += hit ? 1u : 0u;
@@ -237,6 +239,8 @@ __device__ __forceinline__ void flush_stats(unsigned long long *stats, const Lan
     }
     const uint32_t ps = __reduce_add_sync(mask, st.prop_skip);
     if (lane == leader && ps) atomicAdd(stats + LYAP_STAT_PROPOSAL_SKIPPED, (unsigned long long)ps);
+    const uint32_t pr = __reduce_add_sync(mask, st.prop_rej);
+    if (lane == leader && pr) atomicAdd(stats + LYAP_STAT_PROPOSAL_REWOUND, (unsigned long long)pr);
     if (lane == leader && st.rounds) {
         atomicAdd(stats + LYAP_STAT_ROUNDS, (unsigned long long)st.rounds);
         atomicAdd(stats + LYAP_STAT_LANE_ROUNDS, (unsigned long long)st.lane_rounds);
@@ -256,6 +260,45 @@ __device__ __forceinline__ bool known_ahead(const Ray &r, bool fixed_step)
 {
     return (fixed_step && r.phase <= PH_MARCH) || (r.phase >= PH_NORM0 && r.phase < PH_NORM0 + 5) ||
            (r.phase == PH_HONE && r.nh >= HONE_AHEAD);
+}
+
+// What a lane needs of another lane's ray to take samples ahead for it.
+struct AheadState {
+    V3 P, V, QdV;
+    float dt, mag, t, t1;
+    uint32_t phase, nm, cap, noskip;
+};
+
+__device__ __forceinline__ AheadState ahead_state(const Ray &r)
+{
+    return AheadState{r.P, r.V, r.QdV, r.dt, r.mag, r.t, r.t1, r.phase, r.nm, r.cap, r.pnoskip};
+}
+
+// lane `src`'s AheadState (the march bookkeeping only with a proposal)
+template <bool PROP>
+__device__ __forceinline__ AheadState shfl_ahead(const AheadState &a, uint32_t src)
+{
+    AheadState o;
+    o.P.x = __shfl_sync(FULL, a.P.x, src);
+    o.P.y = __shfl_sync(FULL, a.P.y, src);
+    o.P.z = __shfl_sync(FULL, a.P.z, src);
+    o.V.x = __shfl_sync(FULL, a.V.x, src);
+    o.V.y = __shfl_sync(FULL, a.V.y, src);
+    o.V.z = __shfl_sync(FULL, a.V.z, src);
+    o.QdV.x = __shfl_sync(FULL, a.QdV.x, src);
+    o.QdV.y = __shfl_sync(FULL, a.QdV.y, src);
+    o.QdV.z = __shfl_sync(FULL, a.QdV.z, src);
+    o.dt = __shfl_sync(FULL, a.dt, src);
+    o.mag = __shfl_sync(FULL, a.mag, src);
+    o.phase = __shfl_sync(FULL, a.phase, src);
+    if constexpr (PROP) {
+        o.t = __shfl_sync(FULL, a.t, src);
+        o.t1 = __shfl_sync(FULL, a.t1, src);
+        o.nm = __shfl_sync(FULL, a.nm, src);
+        o.cap = __shfl_sync(FULL, a.cap, src);
+        o.noskip = __shfl_sync(FULL, a.noskip, src);
+    }
+    return o;
 }
 
 // The sample `offset` positions ahead of the one at P: march steps and hone
@@ -283,11 +326,25 @@ __device__ __forceinline__ V3 sample_ahead(V3 P, V3 V, float dt, float mag, V3 Q
     return ray_sample_point(tmp);
 }
 
+// sample_ahead for the ray described by `a`.  PROP: the march positions skip
+// the proposal's runs as the ray will (prop_march_ahead).
+template <bool PROP>
+__device__ __forceinline__ V3 sample_ahead(const AheadState &a, const PropGrid &pg, uint32_t offset, bool &valid)
+{
+    if constexpr (PROP) {
+        if (a.phase <= PH_MARCH)
+            return prop_march_ahead(a.P, a.V, a.dt, a.t, a.t1, a.nm, a.cap, a.noskip, pg, offset, valid);
+    }
+    return sample_ahead(a.P, a.V, a.dt, a.mag, a.QdV, a.phase, offset, valid);
+}
+
 // is the ray still where a sample taken ahead in phase `kind` at the round's
 // start (hone step qdt0) continues it?
-__device__ __forceinline__ bool still_ahead(const Ray &r, uint32_t kind, float qdt0)
+// gen0: the ray's proposal rewind count at the round's start (a rewind sends
+// the march back, and the samples taken ahead no longer continue it).
+__device__ __forceinline__ bool still_ahead(const Ray &r, uint32_t kind, float qdt0, uint32_t gen0)
 {
-    return kind == 1u ? r.phase == PH_MARCH
+    return kind == 1u ? (r.phase == PH_MARCH && r.pgen == gen0)
                       : kind == 2u ? r.phase >= PH_NORM0 : (kind == 3u && r.phase == PH_HONE && r.Qdt == qdt0);
 }
 
@@ -306,14 +363,15 @@ __device__ __forceinline__ uint32_t sample_kind(const Ray &r)
 // evaluate, for the rays still running in this warp, the samples those rays
 // will ask for next.  That is only possible where the next positions do not
 // depend on the lambdas still to come: march steps when the step length is
-// fixed (no jitter, near multiplier 1), and the six normal samples.  Helper
-// lane (owner, j) takes the owner's j-th sample ahead; the owner feeds the
-// results to its state machine in order and drops the rest once the ray
-// leaves that phase.
-template <class Lam>
+// fixed (no jitter, near multiplier 1; with a proposal, the runs it skips
+// are a function of the position and so known too), and the six normal
+// samples.  Helper lane (owner, j) takes the owner's j-th sample ahead; the
+// owner feeds the results to its state machine in order and drops the rest
+// once the ray leaves that phase (or a proposal run is rewound).
+template <bool PROP, class Lam>
 __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uint32_t amask, const Lam &lam,
                                             const LyapParams &prm, const bool spec_ok, const bool bracket_mode,
-                                            LaneStats &st)
+                                            const PropGrid &pg, LaneStats &st)
 {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float slot_l[ROUND_WARPS][32];
@@ -340,23 +398,10 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     V3 Q = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
     if (ne) {
         // every lane reads its owner's state (its own, for non-helpers)
-        V3 oP, oV;
-        oP.x = __shfl_sync(FULL, r.P.x, owner);
-        oP.y = __shfl_sync(FULL, r.P.y, owner);
-        oP.z = __shfl_sync(FULL, r.P.z, owner);
-        oV.x = __shfl_sync(FULL, r.V.x, owner);
-        oV.y = __shfl_sync(FULL, r.V.y, owner);
-        oV.z = __shfl_sync(FULL, r.V.z, owner);
-        const float odt = __shfl_sync(FULL, r.dt, owner);
-        const float omag = __shfl_sync(FULL, r.mag, owner);
-        const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
-        V3 oQ;
-        oQ.x = __shfl_sync(FULL, r.QdV.x, owner);
-        oQ.y = __shfl_sync(FULL, r.QdV.y, owner);
-        oQ.z = __shfl_sync(FULL, r.QdV.z, owner);
+        const AheadState o = shfl_ahead<PROP>(ahead_state(r), owner);
         if (helper) {
             bool v;
-            Q = sample_ahead(oP, oV, odt, omag, oQ, ophase, offset, v);
+            Q = sample_ahead<PROP>(o, pg, offset, v);
             st.spec += 1;
         }
     }
@@ -379,6 +424,7 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     if (active) {
         const uint32_t kind = sample_kind(r);   // 1: march, 2: normal, 3: hone
         const float qdt0 = r.Qdt;
+        const uint32_t gen0 = r.pgen;
         // this ray's helpers: ranks idx, idx + ne, ... below ni, one sample each
         uint32_t idx = 0, nh = 0;
         if (ne && ((emask >> lane) & 1u)) {
@@ -393,8 +439,8 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
             st.skipped += bits & 1u;
             st.fallback += (bits >> 1) & 1u;
             st.spec_used += j ? 1u : 0u;
-            res = ray_advance(r, l, prm, bracket_mode);
-            if (res != RAY_CONTINUE || j >= nh || !still_ahead(r, kind, qdt0)) break;
+            res = ray_advance<PROP>(r, l, prm, bracket_mode, &pg);
+            if (res != RAY_CONTINUE || j >= nh || !still_ahead(r, kind, qdt0, gen0)) break;
             l = slot_l[warp][j * ne + idx];
             bits = slot_b[warp][j * ne + idx];
         }
@@ -406,15 +452,15 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
 // per round as one packed evaluation (Lam::eval<2>; the product form runs both
 // on FP32 pairs, fma.rn.f32x2).  Slot 0 is what sample_round evaluates; slot 1
 // is the same ray's next sample when its position is already known -- the
-// next march step when the step length is fixed and no proposal is active, or
-// the next normal sample -- else a dummy.  Lanes without a ray take the next
-// samples of running rays two at a time: helper (owner, j) evaluates the
-// owner's samples 2j and 2j+1 ahead.  The rays consume the results in order,
-// exactly as sample_round does one by one.
-template <class Lam>
+// next march position when the step length is fixed (with a proposal: after
+// the run it skips there), or the next normal sample -- else a dummy.  Lanes
+// without a ray take the next samples of running rays two at a time: helper
+// (owner, j) evaluates the owner's samples 2j and 2j+1 ahead.  The rays
+// consume the results in order, exactly as sample_round does one by one.
+template <bool PROP, class Lam>
 __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, const uint32_t amask, const Lam &lam,
                                                  const LyapParams &prm, const bool fixed_step, const bool spec_ok,
-                                                 const bool bracket_mode, LaneStats &st)
+                                                 const bool bracket_mode, const PropGrid &pg, LaneStats &st)
 {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float2 slot_l[ROUND_WARPS][32];
@@ -448,27 +494,14 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     V3 Q1 = v3(3.0f, 3.0f, 3.0f);
     if (ahead_self) {
         bool v;
-        Q1 = sample_ahead(r.P, r.V, r.dt, r.mag, r.QdV, r.phase, 1u, v);
+        Q1 = sample_ahead<PROP>(ahead_state(r), pg, 1u, v);
     }
     if (ne) {
-        V3 oP, oV;
-        oP.x = __shfl_sync(FULL, r.P.x, owner);
-        oP.y = __shfl_sync(FULL, r.P.y, owner);
-        oP.z = __shfl_sync(FULL, r.P.z, owner);
-        oV.x = __shfl_sync(FULL, r.V.x, owner);
-        oV.y = __shfl_sync(FULL, r.V.y, owner);
-        oV.z = __shfl_sync(FULL, r.V.z, owner);
-        const float odt = __shfl_sync(FULL, r.dt, owner);
-        const float omag = __shfl_sync(FULL, r.mag, owner);
-        const uint32_t ophase = __shfl_sync(FULL, r.phase, owner);
-        V3 oQ;
-        oQ.x = __shfl_sync(FULL, r.QdV.x, owner);
-        oQ.y = __shfl_sync(FULL, r.QdV.y, owner);
-        oQ.z = __shfl_sync(FULL, r.QdV.z, owner);
+        const AheadState o = shfl_ahead<PROP>(ahead_state(r), owner);
         if (helper) {
             bool v0, v1;
-            Q0 = sample_ahead(oP, oV, odt, omag, oQ, ophase, offset, v0);
-            Q1 = sample_ahead(oP, oV, odt, omag, oQ, ophase, offset + 1u, v1);
+            Q0 = sample_ahead<PROP>(o, pg, offset, v0);
+            Q1 = sample_ahead<PROP>(o, pg, offset + 1u, v1);
             st.spec += (v0 ? 1u : 0u) + (v1 ? 1u : 0u);
         }
     }
@@ -492,6 +525,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     if (active) {
         const uint32_t kind = sample_kind(r);   // 1: march, 2: normal, 3: hone
         const float qdt0 = r.Qdt;
+        const uint32_t gen0 = r.pgen;
         // this ray's helpers: ranks idx, idx + ne, ... below ni, two samples each
         uint32_t idx = 0, nh = 0;
         if (ne && ahead) {
@@ -507,14 +541,14 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
             st.skipped += bits & 1u;
             st.fallback += (bits >> 2) & 1u;
             st.spec_used += j ? 1u : 0u;
-            res = ray_advance(r, l0, prm, bracket_mode);
-            if (res != RAY_CONTINUE || !ahead_self || !still_ahead(r, kind, qdt0)) break;
+            res = ray_advance<PROP>(r, l0, prm, bracket_mode, &pg);
+            if (res != RAY_CONTINUE || !ahead_self || !still_ahead(r, kind, qdt0, gen0)) break;
             st.samples += 1;
             st.skipped += (bits >> 1) & 1u;
             st.fallback += (bits >> 3) & 1u;
             st.spec_used += j ? 1u : 0u;
-            res = ray_advance(r, l1, prm, bracket_mode);
-            if (res != RAY_CONTINUE || j >= nh || !still_ahead(r, kind, qdt0)) break;
+            res = ray_advance<PROP>(r, l1, prm, bracket_mode, &pg);
+            if (res != RAY_CONTINUE || j >= nh || !still_ahead(r, kind, qdt0, gen0)) break;
             const float2 v = slot_l[warp][j * ne + idx];
             l0 = v.x;
             l1 = v.y;
@@ -522,44 +556,6 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
         }
     }
     return res;
-}
-
-// Learned proposal: at the start of every march segment the net marked empty
-// the ray takes the segment's steps without evaluating lambda.  Each step is
-// the one ray_advance takes after a sample above the opaque threshold (count
-// the sample, stop at the sample cap, advance t and P, stop past t1), so the
-// samples after a skip sit at exactly the positions the exact march visits.
-// Requires a fixed step length (no jitter, near multiplier 1).  Returns
-// RAY_MISS when the ray leaves the box while skipping.
-__device__ __forceinline__ bool proposal_bit(const uint32_t *row, uint32_t j)
-{
-    return (__ldg(row + (j >> 5)) >> (j & 31u)) & 1u;
-}
-
-__device__ __forceinline__ int proposal_skip(Ray &r, const RenderJob &job, uint32_t pix)
-{
-    const uint32_t G = job.seg_len;
-    const uint32_t *row = job.skip + (size_t)pix * job.skip_words;
-    for (;;) {
-        const uint32_t k = r.nm;
-        if (k % G != 0u) return RAY_CONTINUE;
-        const uint32_t j = k / G;
-        if (j >= job.skip_segments || !proposal_bit(row, j)) return RAY_CONTINUE;
-        if (job.skip_dilate) {
-            if (j > 0u && !proposal_bit(row, j - 1u)) return RAY_CONTINUE;
-            if (j + 1u < job.skip_segments && !proposal_bit(row, j + 1u)) return RAY_CONTINUE;
-        }
-        for (uint32_t s = 0; s < G; s++) {
-            r.nm += 1;
-            r.ns += 1;
-            if (r.nm >= r.cap) return RAY_MISS;
-            r.tprev = r.t;
-            r.t = r.t + r.dt;
-            r.P = r.P + r.V * r.dt;
-            if (r.t > r.t1) return RAY_MISS;
-        }
-        r.phase = PH_MARCH;
-    }
 }
 
 // Queue position qi -> entry.  A ray's cost is set by where it meets the
@@ -595,7 +591,10 @@ struct RenderTuning {
     static constexpr int min_blocks = product ? LYAP_RENDER_MIN_BLOCKS_PRODUCT : LYAP_RENDER_MIN_BLOCKS_PLAIN;
 };
 
-template <class Lam>
+// PROP: the learned proposal's grid (job.prop) decides which march
+// positions are skipped; the host launches this instantiation only with a
+// grid and a fixed step length (jitter 0, near multiplier 1).
+template <class Lam, bool PROP = false>
 __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_blocks)
     render_persistent(const __grid_constant__ RenderJob job, uint32_t *__restrict__ work_counter,
                       unsigned long long *__restrict__ stats)
@@ -607,8 +606,7 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
     const Lam lam(job.seq, job.seq_period, job.prm);
     const CamRays cr = cam_rays(job.cam);
     // march positions are known ahead only with a fixed step length
-    // (with a proposal the march positions depend on its skips: no speculation)
-    const bool fixed_step = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f) && job.skip == nullptr;
+    const bool fixed_step = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f);
     const bool spec_ok = fixed_step && !(job.flags & LYAP_FLAG_NO_SPECULATION);
     const bool bracket_mode = (job.flags & LYAP_FLAG_BISECT_F64) != 0u;
     LaneStats st = {};
@@ -639,13 +637,9 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
                     const uint32_t sx = my % job.width, sy = my / job.width;
                     if (ray_init(r, cr, job.prm, sx, sy)) {
                         active = true;
-                        if (job.skip && proposal_skip(r, job, my) == RAY_MISS) {
-                            finish_pixel(job.rgba, job.points, job.counts, my, r, false, cr.C, job.lights,
-                                         job.n_lights, job.light_model, st);
-                            active = false;
-                        }
                     } else {
                         r.nm = r.nh = r.ns = 0;
+                        r.prej = 0;
                         finish_pixel(job.rgba, job.points, job.counts, my, r, false, cr.C, job.lights,
                                      job.n_lights, job.light_model, st);
                     }
@@ -660,17 +654,11 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
         if (amask == 0) break;
 
         int res;
-        // paired rounds take a ray's next march sample only with a fixed step:
-        // with a proposal's skips the second slot would idle, so one per lane
-        if constexpr (RenderTuning<Lam>::pairs) {
-            if (job.skip == nullptr)
-                res = sample_round_pair(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, st);
-            else
-                res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
-        } else {
-            res = sample_round(r, active, amask, lam, job.prm, spec_ok, bracket_mode, st);
-        }
-        if (active && res == RAY_CONTINUE && job.skip && r.phase == PH_MARCH) res = proposal_skip(r, job, pix);
+        if constexpr (RenderTuning<Lam>::pairs)
+            res = sample_round_pair<PROP>(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, job.prop,
+                                          st);
+        else
+            res = sample_round<PROP>(r, active, amask, lam, job.prm, spec_ok, bracket_mode, job.prop, st);
         if (active && res == RAY_BRACKET) {
             // precision form: hand the crossing to the FP64 bisection pass
             job.bracket[2 * (size_t)pix + 0] = r.tprev;
@@ -688,6 +676,7 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
             }
             st.march += r.nm - r.ns;
             st.prop_skip += r.ns;
+            st.prop_rej += r.prej;
             st.rays += 1;
             active = false;
         } else if (active && res != RAY_CONTINUE) {

@@ -1,7 +1,8 @@
 // lyap_net.cu -- the learned proposal: training of the lambda-predicting MLP
-// on the GPU, its forward pass at arbitrary points, and the proposal pass of
-// a render (which march segments the net calls empty).  No reference
-// counterpart: the reference marches every sample (kernel.cu:326-363).
+// on the GPU, its forward pass at arbitrary points, and the proposal grid a
+// render reads (a lower bound of the net's lambda per cell, built once per
+// net and cached).  No reference counterpart: the reference marches every
+// sample (kernel.cu:326-363).
 //
 // Kernels (all tiles of 128 points, one per thread and per TMEM lane):
 //  * make_samples  -- training set: seeded points uniform in the box, lambda
@@ -13,14 +14,19 @@
 //    K = the tile's 128 points), partial gradients per CTA;
 //  * adam_step     -- sums the CTAs' partials in a fixed order (training is
 //    deterministic) and applies Adam with a cosine learning rate;
-//  * forward_tiles -- the forward pass for the proposal pass (segment
-//    midpoints of the crossing rays) and for lyap_net_eval;
-//  * crossing_rays -- the pixels whose ray meets the box, with t0 and the step.
+//  * forward_tiles -- the forward pass at the corners of the proposal grid,
+//    at the held-out samples, and for lyap_net_eval;
+//  * grid_cells / grid_dilate -- per cell of the proposal grid the minimum
+//    of the net at its 8 corners (any NaN: -inf), optionally the minimum
+//    over the 27 cells around it.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "lyap_internal.h"
@@ -488,70 +494,74 @@ struct SampleSrc {
     }
 };
 
-// ---------------------------------------------------------- proposal pass
-// crossing rays: list[0] = count; entries (pixel, t0, step) as int4 from list + 4
-__global__ void __launch_bounds__(256) crossing_rays(const __grid_constant__ RenderJob job, uint32_t *list)
-{
-    const CamRays cr = cam_rays(job.cam);
-    const uint32_t npix = job.width * job.height;
-    const uint32_t lane = threadIdx.x & 31u;
-    int4 *ent = reinterpret_cast<int4 *>(list + 4);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (npix + stride - 1) / stride;
-    for (uint32_t it = 0; it < rounds; it++) {
-        const uint32_t pix = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        Ray r;
-        const bool cross = pix < npix && ray_init(r, cr, job.prm, pix % job.width, pix / job.width);
-        const uint32_t m = __ballot_sync(FULL, cross);
-        if (!m) continue;
-        const uint32_t leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(list, (uint32_t)__popc(m));
-        base = __shfl_sync(FULL, base, leader);
-        if (cross)
-            ent[base + __popc(m & ((1u << lane) - 1u))] =
-                make_int4((int)pix, __float_as_int(r.t), __float_as_int(r.Fdt), 0);
-    }
-}
-
-struct ProposalSrc {
+// ---------------------------------------------------------- proposal grid
+// the corners of an n^3 grid over the net's box: (n + 1)^3 points, x fastest
+struct GridSrc {
     static constexpr int POINT_STAT = LYAP_STAT_PROPOSAL_POINTS;
-    CamRays cr;
-    const uint32_t *list;
-    uint32_t *mask;
-    uint32_t width, nseg, seg_pad, words, G;
-    float lo[3], inv[3];
-    float tau;
-    __device__ uint64_t tiles() const { return ((uint64_t)list[0] * seg_pad + TILE - 1) / TILE; }
+    float *out;
+    uint32_t m;   // corners per axis (n + 1)
+    uint64_t total;
+    __device__ uint64_t tiles() const { return (total + TILE - 1) / TILE; }
     __device__ bool point(uint64_t p, float &u0, float &u1, float &u2) const
     {
         u0 = u1 = u2 = 0.5f;
-        const uint64_t ri = p / seg_pad;
-        const uint32_t j = (uint32_t)(p % seg_pad);
-        if (ri >= list[0] || j >= nseg) return false;
-        const int4 e = reinterpret_cast<const int4 *>(list + 4)[ri];
-        const uint32_t pix = (uint32_t)e.x;
-        // the ray as ray_init sets it up; the segment's middle sample
-        V3 V = (cr.S0 + cr.SDX * (float)(pix % width)) + cr.SDY * (float)(pix / width);
-        V = normalized(V);
-        V = V / cr.M;
-        const float t = __int_as_float(e.y) + __int_as_float(e.z) * (float)(j * G + G / 2);
-        const V3 P = cr.C + V * t;
-        u0 = (P.x - lo[0]) * inv[0];
-        u1 = (P.y - lo[1]) * inv[1];
-        u2 = (P.z - lo[2]) * inv[2];
+        if (p >= total) return false;
+        const uint64_t mm = (uint64_t)m * m;
+        const uint32_t k = (uint32_t)(p / mm);
+        const uint32_t j = (uint32_t)((p - (uint64_t)k * mm) / m);
+        const uint32_t i = (uint32_t)(p - (uint64_t)k * mm - (uint64_t)j * m);
+        const float inv = 1.0f / (float)(m - 1);
+        u0 = (float)i * inv;
+        u1 = (float)j * inv;
+        u2 = (float)k * inv;
         return true;
     }
     __device__ void result(uint64_t p, bool valid, float o) const
     {
-        const uint32_t bits = __ballot_sync(FULL, valid && o >= tau);
-        const uint64_t ri = p / seg_pad;
-        if ((threadIdx.x & 31u) == 0 && ri < list[0]) {
-            const uint32_t pix = (uint32_t)reinterpret_cast<const int4 *>(list + 4)[ri].x;
-            mask[(size_t)pix * words + (uint32_t)(p % seg_pad) / 32u] = bits;
-        }
+        if (valid) out[p] = o;
     }
 };
+
+// cell (i, j, k) of n^3 = min of the net at its 8 corners; a NaN corner
+// makes the cell -inf (never skipped)
+__global__ void __launch_bounds__(256) grid_cells(const float *__restrict__ corner, float *__restrict__ cell,
+                                                  uint32_t n)
+{
+    const uint64_t total = (uint64_t)n * n * n;
+    const uint64_t m = n + 1;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t nn = (uint64_t)n * n;
+        const uint64_t k = c / nn, j = (c - k * nn) / n, i = c - k * nn - j * n;
+        float v = __int_as_float(0x7f800000);
+#pragma unroll
+        for (int d = 0; d < 8; d++) {
+            const float x = corner[((k + (d >> 2)) * m + (j + ((d >> 1) & 1))) * m + (i + (d & 1))];
+            v = (x == x) ? fminf(v, x) : __int_as_float(0xff800000);
+        }
+        cell[c] = v;
+    }
+}
+
+// the minimum over the (up to) 27 cells around each cell
+__global__ void __launch_bounds__(256) grid_dilate(const float *__restrict__ in, float *__restrict__ out, uint32_t n)
+{
+    const uint64_t total = (uint64_t)n * n * n;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total;
+         c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t nn = (uint64_t)n * n;
+        const int k = (int)(c / nn), j = (int)((c - (uint64_t)k * nn) / n), i = (int)(c - (uint64_t)k * nn - (uint64_t)j * n);
+        float v = __int_as_float(0x7f800000);
+        for (int dk = -1; dk <= 1; dk++)
+            for (int dj = -1; dj <= 1; dj++)
+                for (int di = -1; di <= 1; di++) {
+                    const int kk = k + dk, jj = j + dj, ii = i + di;
+                    if (kk < 0 || jj < 0 || ii < 0 || kk >= (int)n || jj >= (int)n || ii >= (int)n) continue;
+                    v = fminf(v, in[((uint64_t)kk * n + jj) * n + ii]);
+                }
+        out[c] = v;
+    }
+}
 
 static bool g_attr_done[64];
 
@@ -569,7 +579,7 @@ static cudaError_t set_smem_attrs()
         e = cudaFuncSetAttribute(forward_tiles<SampleSrc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)FwdLayout::BYTES);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(forward_tiles<ProposalSrc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(forward_tiles<GridSrc>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)FwdLayout::BYTES);
     if (e == cudaSuccess && dev >= 0 && dev < 64) g_attr_done[dev] = true;
     return e;
@@ -583,82 +593,8 @@ static uint32_t fwd_grid(uint64_t tiles)
 
 }  // namespace net
 
-// ------------------------------------------------ proposal pass (lyap_render)
-uint32_t proposal_segments(const LyapParams &prm, uint32_t seg_len, uint32_t *words)
-{
-    const float d = prm.depth / (float)seg_len;
-    uint32_t nseg = (d >= 1.0f) ? (d < 2048.0f ? (uint32_t)d : 2048u) : 0u;
-    if (words) *words = (nseg + 31u) / 32u;
-    return nseg;
-}
-
-size_t proposal_scratch_bytes(size_t npix, uint32_t words)
-{
-    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    return up(net::NPARAM * sizeof(float)) + up(16 + npix * 16) + up(npix * words * sizeof(uint32_t));
-}
-
-cudaError_t launch_proposal(RenderJob &job, const LyapNet &netw, float margin, uint32_t seg_len, uint32_t dilate,
-                            void *scratch, unsigned long long *stats, cudaStream_t s)
-{
-    using namespace net;
-    uint32_t words = 0;
-    const uint32_t nseg = proposal_segments(job.prm, seg_len, &words);
-    if (nseg == 0) return cudaSuccess;   // fewer samples than a segment: nothing to skip
-    const size_t npix = (size_t)job.width * job.height;
-    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    char *base = static_cast<char *>(scratch);
-    float *d_params = reinterpret_cast<float *>(base);
-    uint32_t *list = reinterpret_cast<uint32_t *>(base + up(NPARAM * sizeof(float)));
-    uint32_t *mask = reinterpret_cast<uint32_t *>(base + up(NPARAM * sizeof(float)) + up(16 + npix * 16));
-    cudaError_t e = set_smem_attrs();
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d_params, netw.params, NPARAM * sizeof(float), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(list, 0, 16, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(mask, 0, npix * words * sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    const int sms = device_sm_count();
-    if (sms <= 0) return cudaErrorNoDevice;
-    crossing_rays<<<(uint32_t)sms * 8, 256, 0, s>>>(job, list);
-    ProposalSrc src;
-    const LyapCam &c = job.cam;
-    src.cr.C = V3{c.C.x, c.C.y, c.C.z};
-    src.cr.S0 = V3{c.S0.x, c.S0.y, c.S0.z};
-    src.cr.SDX = V3{c.SDX.x, c.SDX.y, c.SDX.z};
-    src.cr.SDY = V3{c.SDY.x, c.SDY.y, c.SDY.z};
-    src.cr.M = c.M;
-    src.list = list;
-    src.mask = mask;
-    src.width = job.width;
-    src.nseg = nseg;
-    src.seg_pad = words * 32u;
-    src.words = words;
-    src.G = seg_len;
-    for (int k = 0; k < 3; k++) {
-        src.lo[k] = netw.lo[k];
-        src.inv[k] = 1.0f / (netw.hi[k] - netw.lo[k]);
-    }
-    src.tau = job.prm.opaqueThreshold + margin;
-    // an upper bound on the tiles (every pixel crossing); CTAs past the real count return at once
-    const uint64_t max_tiles = (npix * src.seg_pad + TILE - 1) / TILE;
-    forward_tiles<ProposalSrc><<<fwd_grid(max_tiles), TILE, FwdLayout::BYTES, s>>>(d_params, src, stats);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    job.skip = mask;
-    job.skip_words = words;
-    job.skip_segments = nseg;
-    job.seg_len = seg_len;
-    job.skip_dilate = dilate;
-    return cudaSuccess;
-}
-
-}  // namespace lyapgb
-
-// ============================================================ C entry points
-using namespace lyapgb;
-using namespace lyapgb::net;
-
-namespace {
-
+// ------------------------------------------------ proposal grid (lyap_render)
+// FNV-1a 64 (LyapNet.hash, and the grid cache's key)
 uint64_t fnv64(const void *p, size_t n)
 {
     const unsigned char *b = static_cast<const unsigned char *>(p);
@@ -669,6 +605,106 @@ uint64_t fnv64(const void *p, size_t n)
     }
     return h;
 }
+
+namespace {
+
+// built grids, per (device, hash of the net's bytes, cells per axis,
+// dilation); kept for the life of the process (kGridsKeep at most, the least
+// recently used dropped).  The hash is computed here, not read from
+// LyapNet.hash, which callers that fill the struct themselves may not set.
+struct GridEntry {
+    float *grid = nullptr;
+    uint64_t order = 0;
+};
+std::mutex g_grid_mu;
+std::map<std::tuple<int, uint64_t, uint32_t, uint32_t>, GridEntry> g_grids;
+uint64_t g_grid_order = 0;
+constexpr size_t kGridsKeep = 8;
+
+}  // namespace
+
+cudaError_t proposal_grid(const LyapNet &netw, uint32_t n, uint32_t dilate, const float **grid,
+                          unsigned long long *stats, cudaStream_t s)
+{
+    using namespace net;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const auto key = std::make_tuple(dev, fnv64(&netw, offsetof(LyapNet, hash)), n, dilate);
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    auto it = g_grids.find(key);
+    if (it != g_grids.end()) {
+        it->second.order = ++g_grid_order;
+        *grid = it->second.grid;
+        return cudaSuccess;
+    }
+    if ((e = set_smem_attrs()) != cudaSuccess) return e;
+    const uint64_t m = (uint64_t)n + 1, ncorner = m * m * m, ncell = (uint64_t)n * n * n;
+    auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    // scratch: the net's parameters, the corner values, and (with dilation) the undilated cells
+    const size_t bytes = up(NPARAM * sizeof(float)) + up(ncorner * sizeof(float)) +
+                         (dilate ? up(ncell * sizeof(float)) : 0);
+    char *tmp = nullptr;
+    float *out = nullptr;
+    if ((e = cudaMalloc((void **)&out, ncell * sizeof(float))) != cudaSuccess) return e;
+    if ((e = scratch_alloc((void **)&tmp, bytes, s)) != cudaSuccess) {
+        cudaFree(out);
+        return e;
+    }
+    float *d_params = reinterpret_cast<float *>(tmp);
+    float *corner = reinterpret_cast<float *>(tmp + up(NPARAM * sizeof(float)));
+    float *undilated = dilate ? reinterpret_cast<float *>(tmp + up(NPARAM * sizeof(float)) +
+                                                          up(ncorner * sizeof(float)))
+                              : out;
+    e = cudaMemcpyAsync(d_params, netw.params, NPARAM * sizeof(float), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+        GridSrc src;
+        src.out = corner;
+        src.m = (uint32_t)m;
+        src.total = ncorner;
+        forward_tiles<GridSrc><<<fwd_grid((ncorner + TILE - 1) / TILE), TILE, FwdLayout::BYTES, s>>>(d_params, src,
+                                                                                                     stats);
+        e = cudaGetLastError();
+    }
+    const uint32_t blocks = (uint32_t)device_sm_count() * 8u;
+    if (e == cudaSuccess) {
+        grid_cells<<<blocks, 256, 0, s>>>(corner, undilated, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && dilate) {
+        grid_dilate<<<blocks, 256, 0, s>>>(undilated, out, n);
+        e = cudaGetLastError();
+    }
+    cudaError_t e2 = cudaFreeAsync(tmp, s);
+    // complete before any stream may read it from the cache
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaFree(out);
+        return e;
+    }
+    if (g_grids.size() >= kGridsKeep) {
+        auto old = g_grids.begin();
+        for (auto jt = g_grids.begin(); jt != g_grids.end(); ++jt)
+            if (jt->second.order < old->second.order) old = jt;
+        cudaFree(old->second.grid);   // synchronises the device: no launch still reads it
+        g_grids.erase(old);
+    }
+    GridEntry ent;
+    ent.grid = out;
+    ent.order = ++g_grid_order;
+    g_grids[key] = ent;
+    *grid = out;
+    return cudaSuccess;
+}
+
+}  // namespace lyapgb
+
+// ============================================================ C entry points
+using namespace lyapgb;
+using namespace lyapgb::net;
+
+namespace {
 
 uint32_t fnv32_add(uint32_t h, const void *p, size_t n)
 {
@@ -889,6 +925,24 @@ extern "C" int lyap_net_train(const LyapParams *prm, const int32_t *seq, size_t 
         }
     }
     return rc;
+}
+
+extern "C" int lyap_net_grid(const LyapNet *netw, uint32_t n, uint32_t dilate, float *d_out, void *stream)
+{
+    const char *fn = "lyap_net_grid";
+    int rc = check_net(netw, fn);
+    if (rc) return rc;
+    if (!d_out) return set_error(LYAP_ERR_INVALID_ARG, "%s: null output", fn);
+    if (n == 0) n = LYAP_PROPOSAL_GRID_DEFAULT;
+    if (n < 2 || n > 512) return set_error(LYAP_ERR_INVALID_ARG, "%s: %u cells per axis outside 2..512", fn, n);
+    if (dilate > 1) return set_error(LYAP_ERR_INVALID_ARG, "%s: dilate must be 0 or 1", fn);
+    if (device_sm_count() <= 0) return cuda_error(cudaErrorNoDevice, fn);
+    cudaStream_t s = (cudaStream_t)stream;
+    const float *grid = nullptr;
+    cudaError_t e = proposal_grid(*netw, n, dilate, &grid, nullptr, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_out, grid, (size_t)n * n * n * sizeof(float), cudaMemcpyDeviceToDevice, s);
+    return e == cudaSuccess ? LYAP_OK : cuda_error(e, fn);
 }
 
 extern "C" int lyap_net_eval(const LyapNet *netw, const float *d_xyz, size_t n, float *d_out, void *stream)

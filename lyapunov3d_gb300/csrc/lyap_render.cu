@@ -33,10 +33,19 @@ cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_
     if (threads == 0) threads = LYAP_RENDER_THREADS;
     if (blocks_per_sm == 0) blocks_per_sm = LYAP_RENDER_MIN_BLOCKS;
     const uint32_t grid = (uint32_t)sms * blocks_per_sm;
-    if (mode == MODE_PRODUCT)
-        render_persistent<RuntimeLambda<MODE_PRODUCT>><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
-    else
-        render_persistent<RuntimeLambda<MODE_PLAIN>><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
+    const bool prop = job.prop.grid != nullptr;   // the learned proposal's instantiation
+    if (mode == MODE_PRODUCT) {
+        if (prop)
+            render_persistent<RuntimeLambda<MODE_PRODUCT>, true>
+                <<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
+        else
+            render_persistent<RuntimeLambda<MODE_PRODUCT>><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
+    } else {
+        if (prop)
+            render_persistent<RuntimeLambda<MODE_PLAIN>, true><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
+        else
+            render_persistent<RuntimeLambda<MODE_PLAIN>><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
+    }
     return cudaGetLastError();
 }
 

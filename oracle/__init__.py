@@ -76,6 +76,8 @@ class Oracle:
         L.orc_lights_recalculate.argtypes = [c_void_p, c_size_t]
         L.orc_cam_recalculate_d.argtypes = [c_void_p, c_uint32, c_uint32, c_uint32]
         L.orc_lights_recalculate_d.argtypes = [c_void_p, c_size_t]
+        L.orc_render_rows_prop.argtypes = [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                           c_uint32, c_uint32, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]
         L.orc_set_threads.argtypes = [c_int]
         L.orc_get_threads.restype = c_int
 
@@ -161,6 +163,24 @@ class Oracle:
         self.lib.orc_shade(ctypes.byref(pt), ctypes.byref(cam), arr, len(lights), col, ctypes.byref(px))
         return tuple(col), (px.r, px.g, px.b, px.a)
 
+    def render_prop(self, mode, w, h, cam, prm, seq, lights, prop, y0=0, y1=None):
+        """render() with the product's proposal march (prop: from proposal());
+        also returns pcounts[h', w, 2] (skipped positions, rewound runs)."""
+        y1 = h if y1 is None else y1
+        s = _seq_array(seq)
+        rgba = np.zeros((y1 - y0) * w, dtype=RGBA_DTYPE)
+        pts = np.zeros((y1 - y0) * w, dtype=POINT_DTYPE)
+        cnt = np.zeros((y1 - y0) * w * 3, dtype=np.uint32)
+        pcnt = np.zeros((y1 - y0) * w * 2, dtype=np.uint32)
+        arr = (LyapLight * max(1, len(lights)))(*[LyapLight.from_buffer_copy(l) for l in lights])
+        off = y0 * w
+        self.lib.orc_render_rows_prop(mode, c_void_p(rgba.ctypes.data - off * 4), c_void_p(pts.ctypes.data - off * 36),
+                                      ctypes.byref(cam), ctypes.byref(prm), _ptr(s), arr, len(lights), w, y0, y1,
+                                      ctypes.byref(prop[0]), c_void_p(cnt.ctypes.data - off * 12),
+                                      c_void_p(pcnt.ctypes.data - off * 8))
+        return (rgba.view(np.uint8).reshape(y1 - y0, w, 4), pts.reshape(y1 - y0, w), cnt.reshape(y1 - y0, w, 3),
+                pcnt.reshape(y1 - y0, w, 2))
+
     def render(self, mode, w, h, cam, prm, seq, lights, y0=0, y1=None):
         """Rows [y0, y1) of a w-wide image: (rgba[h', w, 4] u8, points[h', w], counts[h', w, 3])."""
         y1 = h if y1 is None else y1
@@ -180,6 +200,26 @@ class Oracle:
                                  c_void_p(base_cnt))
         return (rgba.view(np.uint8).reshape(y1 - y0, w, 4), pts.reshape(y1 - y0, w),
                 cnt.reshape(y1 - y0, w, 3))
+
+
+class OrcProposal(ctypes.Structure):
+    """lyap_oracle.h OrcProposal: the product's proposal grid as its march reads it."""
+    _fields_ = [("grid", c_void_p), ("n", c_uint32), ("run", c_uint32), ("lo", c_float * 3), ("scale", c_float * 3),
+                ("tau", c_float)]
+
+
+def proposal(grid, n, run, lo, hi, tau):
+    """An OrcProposal over the box [lo, hi] (the net's) for a grid of n^3
+    float32 cells (kept alive by the returned tuple's second item)."""
+    g = np.ascontiguousarray(np.asarray(grid, dtype=np.float32).reshape(-1))
+    assert g.size == n ** 3
+    p = OrcProposal()
+    p.grid = g.ctypes.data
+    p.n, p.run, p.tau = n, run, tau
+    for k in range(3):
+        p.lo[k] = lo[k]
+        p.scale[k] = np.float32(n) / (np.float32(hi[k]) - np.float32(lo[k]))
+    return p, g
 
 
 def params_to_double(p):

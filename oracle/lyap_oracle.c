@@ -245,6 +245,19 @@ void orc_lyap4d_batch(int mode, const double *pts, size_t n, uint32_t settle,
     }
 }
 
+/* The proposal grid lookup of the product's march (prop_skippable in
+ * lyap_device.cuh), in float: cell = (P - lo) * scale, truncated. */
+static int orc_prop_skippable(const OrcProposal *p, float x, float y, float z)
+{
+    const float nf = (float)p->n;
+    const float fx = (x - p->lo[0]) * p->scale[0];
+    const float fy = (y - p->lo[1]) * p->scale[1];
+    const float fz = (z - p->lo[2]) * p->scale[2];
+    if (!(fx >= 0.0f && fx < nf && fy >= 0.0f && fy < nf && fz >= 0.0f && fz < nf)) return 0;
+    const uint32_t ix = (uint32_t)fx, iy = (uint32_t)fy, iz = (uint32_t)fz;
+    return p->grid[((size_t)iz * p->n + iy) * p->n + ix] >= p->tau;
+}
+
 /* ---- the two instantiations of oracle_impl.h ---------------------------- */
 #define R float
 #define SFX(name) name##_f
@@ -300,12 +313,18 @@ void orc_lights_recalculate_d(LyapLightD *lights, size_t n)
 int orc_raymarch(int mode, LyapPoint *pt, uint32_t sx, uint32_t sy,
                  const LyapCam *cam, const LyapParams *prm,
                  const int32_t *seq, uint32_t *counts)
-{ return orc_raymarch_impl_f(mode, pt, sx, sy, cam, prm, seq, counts); }
+{ return orc_raymarch_impl_f(mode, pt, sx, sy, cam, prm, seq, counts, NULL, NULL); }
+
+int orc_raymarch_prop(int mode, LyapPoint *pt, uint32_t sx, uint32_t sy,
+                      const LyapCam *cam, const LyapParams *prm,
+                      const int32_t *seq, const OrcProposal *prop,
+                      uint32_t *counts, uint32_t *pcounts)
+{ return orc_raymarch_impl_f(mode, pt, sx, sy, cam, prm, seq, counts, prop, pcounts); }
 
 int orc_raymarch_d(LyapPointD *pt, uint32_t sx, uint32_t sy,
                    const LyapCamD *cam, const LyapParamsD *prm,
                    const int32_t *seq, uint32_t *counts)
-{ return orc_raymarch_impl_d(0, pt, sx, sy, cam, prm, seq, counts); }
+{ return orc_raymarch_impl_d(0, pt, sx, sy, cam, prm, seq, counts, NULL, NULL); }
 
 /* ---- shade (kernel.cu:25-106) and the byte conversion ------------------- */
 
@@ -381,15 +400,28 @@ void orc_render_rows(int mode, RGBA *rgba, LyapPoint *points,
                      uint32_t n_lights, uint32_t w, uint32_t y0, uint32_t y1,
                      uint32_t *counts)
 {
+    orc_render_rows_prop(mode, rgba, points, cam, prm, seq, lights, n_lights, w, y0, y1, NULL, counts, NULL);
+}
+
+void orc_render_rows_prop(int mode, RGBA *rgba, LyapPoint *points,
+                          const LyapCam *cam, const LyapParams *prm,
+                          const int32_t *seq, const LyapLight *lights,
+                          uint32_t n_lights, uint32_t w, uint32_t y0, uint32_t y1,
+                          const OrcProposal *prop, uint32_t *counts, uint32_t *pcounts)
+{
     long long n = (long long)w * (long long)(y1 - y0);
     #pragma omp parallel for schedule(dynamic, 16) OMP_THREADS
     for (long long k = 0; k < n; k++) {
         uint32_t x = (uint32_t)(k % w), y = y0 + (uint32_t)(k / w);
         size_t ind = (size_t)x + (size_t)y * w;
         LyapPoint pt;
-        uint32_t cnt[3];
-        if (orc_raymarch(mode, &pt, x, y, cam, prm, seq, cnt) != 0)
+        uint32_t cnt[3], pc[2];
+        if (orc_raymarch_impl_f(mode, &pt, x, y, cam, prm, seq, cnt, prop, pc) != 0)
             memset(&pt, 0xff, sizeof(pt));
+        if (pcounts) {
+            pcounts[2 * ind + 0] = pc[0];
+            pcounts[2 * ind + 1] = pc[1];
+        }
         points[ind] = pt;
         orc_shade(&pt, cam, lights, n_lights, NULL, &rgba[ind]);
         if (counts) {

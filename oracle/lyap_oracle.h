@@ -108,6 +108,32 @@ void orc_render_rows(int mode, RGBA *rgba, LyapPoint *points,
                      uint32_t n_lights, uint32_t w, uint32_t y0, uint32_t y1,
                      uint32_t *counts);
 
+/* The product's learned-proposal march (not the reference's: it has no
+ * proposal), restated so that the GPU's proposal path has a checker: a
+ * grid of n^3 cells (x fastest) over the box lo + [0, n / scale) with a
+ * lower bound of the net's lambda per cell (lyap_net_grid writes it), the
+ * skip / confirm threshold tau and the longest skipped run. */
+typedef struct {
+    const float *grid;
+    uint32_t n, run;
+    float lo[3], scale[3];
+    float tau;
+} OrcProposal;
+
+/* orc_raymarch with the proposal; counts[0] = evaluated march samples,
+ * pcounts[0..1] = skipped positions, rewound runs (either may be NULL). */
+int orc_raymarch_prop(int mode, LyapPoint *pt, uint32_t sx, uint32_t sy,
+                      const LyapCam *cam, const LyapParams *prm,
+                      const int32_t *seq, const OrcProposal *prop,
+                      uint32_t *counts, uint32_t *pcounts);
+/* orc_render_rows with the proposal (prop NULL: orc_render_rows);
+ * pcounts: 2 per pixel, may be NULL. */
+void orc_render_rows_prop(int mode, RGBA *rgba, LyapPoint *points,
+                          const LyapCam *cam, const LyapParams *prm,
+                          const int32_t *seq, const LyapLight *lights,
+                          uint32_t n_lights, uint32_t w, uint32_t y0, uint32_t y1,
+                          const OrcProposal *prop, uint32_t *counts, uint32_t *pcounts);
+
 /* Threads the OpenMP loops use (0 = runtime default). */
 void orc_set_threads(int n);
 int orc_get_threads(void);

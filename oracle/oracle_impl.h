@@ -116,13 +116,27 @@ void SFX(orc_cam_recalculate_impl)(CAM *cam, uint32_t tw, uint32_t th, uint32_t 
 }
 
 /* ---- raymarch (kernel.cu:156-486) --------------------------------------- */
+/* prop (float instantiation only; NULL = the reference's march): the
+ * product's learned-proposal march, restated for its own parity check --
+ * after every march step, a run of up to prop->run positions whose grid
+ * cell holds a value >= prop->tau is skipped (never the last position before
+ * t1 or the cap); the position after the run is evaluated and confirms it
+ * when its lambda is above prop->tau, else every position from the run's
+ * first through the confirming one is evaluated exactly.  counts[0] is then
+ * the evaluated march samples; pcounts (may be NULL) receives the skipped
+ * positions and the rewound runs. */
 int SFX(orc_raymarch_impl)(int mode, POINT *point, uint32_t sx, uint32_t sy,
                            const CAM *cam, const PARAMS *prm,
-                           const int32_t *seq, uint32_t *counts)
+                           const int32_t *seq, uint32_t *counts,
+                           const OrcProposal *prop, uint32_t *pcounts)
 {
     uint32_t nm = 0, nh = 0, nn = 0;
+    uint32_t ns = 0, nrew = 0, noskip = 0;   /* proposal: skipped, rewound, exact until */
     (void)mode;
     if (counts) counts[0] = counts[1] = counts[2] = 0;
+    if (pcounts) pcounts[0] = pcounts[1] = 0;
+#define ORC_COUNTS() do { if (counts) { counts[0] = nm - ns; counts[1] = nh; counts[2] = nn; } \
+                          if (pcounts) { pcounts[0] = ns; pcounts[1] = nrew; } } while (0)
 
     VEC V = SFX(vadd)(SFX(vadd)(cam->S0, SFX(vscale)(cam->SDX, (R)sx)), SFX(vscale)(cam->SDY, (R)sy));
     V = SFX(vnormalized)(V);
@@ -202,7 +216,7 @@ int SFX(orc_raymarch_impl)(int mode, POINT *point, uint32_t sx, uint32_t sy,
 
     while (l > prm->opaqueThreshold) {
         if (nm >= cap) {
-            if (counts) { counts[0] = nm; counts[1] = nh; counts[2] = nn; }
+            ORC_COUNTS();
             return 1;
         }
         if (prm->jitter != 0.0) {
@@ -223,8 +237,40 @@ int SFX(orc_raymarch_impl)(int mode, POINT *point, uint32_t sx, uint32_t sy,
             P = SFX(vadd)(P, SFX(vscale)(V, dt));
         }
         if (t > t1) {
-            if (counts) { counts[0] = nm; counts[1] = nh; counts[2] = nn; }
+            ORC_COUNTS();
             return 1;
+        }
+        if (prop && nm >= noskip) {
+            uint32_t k = 0;
+            VEC Q = P;
+            R tq = t;
+            while (k < prop->run && nm + k + 1 < cap && orc_prop_skippable(prop, (float)Q.x, (float)Q.y, (float)Q.z)) {
+                R tn = tq + dt;
+                if (tn > t1) break;
+                tq = tn;
+                Q = SFX(vadd)(Q, SFX(vscale)(V, dt));
+                k++;
+            }
+            if (k) {
+                R lc = LAMBDA(Q, prm->d);
+                if (lc > prop->tau) {
+                    /* confirmed: the run is skipped, lc is the march sample at Q */
+                    P = Q;
+                    t = tq;
+                    nm += k;
+                    ns += k;
+                    l = lc;
+                    nm++;
+                    if (l > prm->chaosThreshold)
+                        c += l;
+                    else if (l > prm->opaqueThreshold)
+                        a += l;
+                    continue;
+                }
+                /* rewound: march exactly through the confirming position */
+                noskip = nm + k + 1;
+                nrew++;
+            }
         }
         l = LAMBDA(P, prm->d); nm++;
         if (l > prm->chaosThreshold)
@@ -240,7 +286,7 @@ int SFX(orc_raymarch_impl)(int mode, POINT *point, uint32_t sx, uint32_t sy,
         }
     }
     if (t > t1) {
-        if (counts) { counts[0] = nm; counts[1] = nh; counts[2] = nn; }
+        ORC_COUNTS();
         return 1;
     }
 
@@ -290,6 +336,7 @@ int SFX(orc_raymarch_impl)(int mode, POINT *point, uint32_t sx, uint32_t sy,
     point->a = a;
     point->c = c;
     point->l = l;
-    if (counts) { counts[0] = nm; counts[1] = nh; counts[2] = nn; }
+    ORC_COUNTS();
     return 0;
+#undef ORC_COUNTS
 }

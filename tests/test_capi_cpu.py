@@ -194,7 +194,7 @@ def test_abi_struct_sizes_match_c(tmp_path):
         pytest.skip("gcc not available")
     checks = {
         "LyapRenderExt": (capi.LyapRenderExt, ["size", "flags", "d_counts", "d_stats", "h_seq", "bisect_halvings",
-                                               "proposal", "proposal_margin", "proposal_dilate", "pad2_"]),
+                                               "proposal", "proposal_margin", "proposal_dilate", "proposal_grid"]),
         "LyapNet": (capi.LyapNet, ["lo", "hi", "params", "train_mse", "val_mse", "seq_hash", "hash"]),
         "LyapNetTrainOptions": (capi.LyapNetTrainOptions, ["steps", "lr", "seed", "box_lo", "box_hi", "h_loss"]),
         "LyapVolumeExt": (capi.LyapVolumeExt, ["variant", "d_stats", "flags", "h_seq"]),
