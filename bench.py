@@ -761,13 +761,35 @@ def run_proposal_report(args):
             ts.append(e0.elapsed_time(e1))
         return statistics.median(ts), frame.stats() // max(1, args.steps), frame.d_points.view(-1, 9).cpu().numpy()
 
+    mask64 = (1 << 64) - 1
+
+    def kernel_times(st):
+        """the render launch's own span and its share after the queue drained (%globaltimer)"""
+        t0_, td, te = (~int(st[capi.STAT_T_START])) & mask64, (~int(st[capi.STAT_T_DRAIN])) & mask64, \
+            int(st[capi.STAT_T_END])
+        if not te > td > t0_:
+            return {}
+        return {"kernel_ms": (te - t0_) / 1e6, "after_drain_ms": (te - td) / 1e6,
+                "rounds": int(st[capi.STAT_ROUNDS]),
+                "lane_utilisation": float(st[capi.STAT_LANE_ROUNDS]) / max(1.0, 32.0 * float(st[capi.STAT_ROUNDS]))}
+
+    def timed_kernel(**kw):
+        """one more frame with the statistics of that frame alone (start / drain / end stamps)"""
+        frame.reset_stats()
+        frame.run(capi.VARIANT_PRODUCT, stream=stream, jit=True, **kw)
+        torch.cuda.synchronize()
+        return kernel_times(frame.stats())
+
     ms0, st0, p0 = timed()
+    k0 = timed_kernel()
     hit0 = ~np.isnan(p0[:, 0])
     rows = []
     for which, nt in (("trained", net), ("untrained", untrained)):
         for m in (float(x) for x in args.margins.split(",")):
-            ms, st, p1 = timed(proposal=ctypes.pointer(nt), proposal_margin=m, proposal_segment=args.proposal_segment,
-                               proposal_grid=n, proposal_dilate=args.proposal_dilate)
+            kw = dict(proposal=ctypes.pointer(nt), proposal_margin=m, proposal_segment=args.proposal_segment,
+                      proposal_grid=n, proposal_dilate=args.proposal_dilate)
+            ms, st, p1 = timed(**kw)
+            kt = timed_kernel(**kw)
             hit1 = ~np.isnan(p1[:, 0])
             same = hit0 & hit1 & (p0[:, :3].view(np.uint32) == p1[:, :3].view(np.uint32)).all(1)
             rows.append({"net": which, "margin": m, "ms": ms, "speedup": ms0 / ms,
@@ -777,7 +799,7 @@ def run_proposal_report(args):
                          "net_timeouts": int(st[capi.STAT_NET_TIMEOUTS]),
                          "surface_agreement": float(hit1.sum() / max(1, hit0.sum())),
                          "same_sample_agreement": float(same.sum() / max(1, hit0.sum())),
-                         "extra_hits": int((hit1 & ~hit0).sum())})
+                         "extra_hits": int((hit1 & ~hit0).sum()), "kernel": kt})
     print(json.dumps({
         "report": "proposal", "workload": wl.name, "width": wl.width, "height": wl.height,
         "train": {"seconds": t_train, "steps": net.steps, "batch": net.batch, "samples": net.n_samples,
@@ -786,7 +808,8 @@ def run_proposal_report(args):
         "grid": {"cells_per_axis": n, "dilate": args.proposal_dilate, "build_s": t_grid,
                  "net_points": (n + 1) ** 3},
         "segment": args.proposal_segment,
-        "without_proposal": {"ms": ms0, "samples": int(st0[capi.STAT_SAMPLES]), "hits": int(hit0.sum())},
+        "without_proposal": {"ms": ms0, "samples": int(st0[capi.STAT_SAMPLES]), "hits": int(hit0.sum()),
+                             "kernel": k0},
         "with_proposal": rows}), flush=True)
 
 

@@ -293,7 +293,10 @@ typedef struct {
     uint32_t proposal_dilate;    /* 0 or 1 */
     uint32_t proposal_grid;      /* cells per axis, 2..512 (0 = LYAP_PROPOSAL_GRID_DEFAULT) */
 } LyapRenderExt;
-#define LYAP_PROPOSAL_GRID_DEFAULT 128u
+#define LYAP_PROPOSAL_GRID_DEFAULT 64u
+/* grids of up to this many bytes of bits (n^3 / 8; 64^3 = 32 KB) are read
+ * from shared memory during the march, larger ones from global memory */
+#define LYAP_PROPOSAL_SMEM_MAX 49152u
 
 typedef struct {
     uint32_t size;               /* = sizeof(LyapVolumeExt) */

@@ -44,7 +44,7 @@ MAX_LIGHTS = 16
  STAT_SPEC_USED, STAT_ROUNDS, STAT_LANE_ROUNDS, STAT_MAX_ROUNDS, STAT_PROPOSAL_SKIPPED, STAT_PROPOSAL_POINTS,
  STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END, STAT_PROPOSAL_REWOUND) = range(20)
 STAT_COUNT = 20
-PROPOSAL_GRID_DEFAULT = 128
+PROPOSAL_GRID_DEFAULT = 64
 # the proposal margin the library's users are pointed to: the smallest of the
 # measured margins at which the 1080p bench frame keeps >= 99.9 % of its
 # surface pixels (bench.py --report proposal)

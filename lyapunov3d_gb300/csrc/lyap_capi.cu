@@ -254,17 +254,20 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
     if (const LyapNet *net = ext_proposal(ext)) {
         const uint32_t n = ext->proposal_grid ? ext->proposal_grid : LYAP_PROPOSAL_GRID_DEFAULT;
         const uint32_t seg = ext->proposal_segment ? ext->proposal_segment : 8u;
-        const float *grid = nullptr;
-        cudaError_t ge = proposal_grid(*net, n, ext->proposal_dilate, &grid, ext->d_stats, s);
+        const float tau = prm->opaqueThreshold + ext->proposal_margin;
+        const uint32_t *bits = nullptr;
+        cudaError_t ge = proposal_bits(*net, n, ext->proposal_dilate, tau, &bits, ext->d_stats, s);
         if (ge != cudaSuccess) return cuda_error(ge, "lyap_render: proposal grid");
-        job.prop.grid = grid;
+        job.prop.bits = bits;
         job.prop.n = n;
         job.prop.run = seg - 1;
         for (int k = 0; k < 3; k++) {
             job.prop.lo[k] = net->lo[k];
             job.prop.scale[k] = (float)n / (net->hi[k] - net->lo[k]);
         }
-        job.prop.tau = prm->opaqueThreshold + ext->proposal_margin;
+        job.prop.tau = tau;
+        const uint64_t words = ((uint64_t)n * n * n + 31) / 32;
+        job.prop.smem_words = words * 4 <= LYAP_PROPOSAL_SMEM_MAX ? (uint32_t)words : 0u;
     }
     // scratch, stream-ordered so concurrent calls on different streams each
     // get their own: a 256-byte header (the queue's counter, the ray list's

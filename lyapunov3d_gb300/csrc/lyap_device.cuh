@@ -880,14 +880,13 @@ struct Ray {
     uint32_t phase, nm, nh, cap;
     uint32_t ns;     // march samples the learned proposal skipped (counted in nm, never evaluated)
     bool near, sign;
-    // learned proposal only (ray_advance<true>): the pending march sample
-    // confirms a run of `prun` skipped positions that began at (Ps, ts, tps);
-    // positions are evaluated exactly while nm < pnoskip; pgen counts the
-    // rewinds (samples taken ahead for this ray are stale once it changes);
-    // prej the samples a rewind discarded
-    V3 Ps;
-    float ts, tps;
-    uint32_t prun, pnoskip, pgen, prej;
+    // learned proposal only (ray_advance<true>): pst packs the run of
+    // skipped positions the pending march sample confirms (bits 0-5: the
+    // sample is that many steps past P, where the ray waits until the run is
+    // confirmed), a rewind counter (bits 6-13: samples taken ahead for this
+    // ray are stale once it changes) and the samples rewinds discarded (bits
+    // 14-31); positions are evaluated exactly while nm < pnoskip
+    uint32_t pst, pnoskip;
 };
 
 struct CamRays {   // the per-frame camera quantities raymarch reads
@@ -904,7 +903,7 @@ __device__ __forceinline__ CamRays cam_rays(const LyapCam &cam)
 // ray misses the box [lMin, lMax]^3 (raymarch returns 1 before any sample).
 __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapParams &prm, uint32_t sx, uint32_t sy)
 {
-    r.prun = r.pnoskip = r.pgen = r.prej = 0;
+    r.pst = r.pnoskip = 0;
     V3 V = (cam.S0 + cam.SDX * (float)sx) + cam.SDY * (float)sy;
     V = normalized(V);
     V = V / cam.M;
@@ -970,8 +969,12 @@ __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapP
 }
 
 // ---------------------------------------------------- the learned proposal
-// Is the march position P in a cell whose lower bound of the net's lambda
-// is at least the skip threshold?  Positions outside the grid never are.
+__device__ __forceinline__ uint32_t prop_run(const Ray &r) { return r.pst & 63u; }
+__device__ __forceinline__ uint32_t prop_gen(const Ray &r) { return (r.pst >> 6) & 255u; }
+__device__ __forceinline__ uint32_t prop_rewound(const Ray &r) { return r.pst >> 14; }
+
+// Is the march position P in a cell whose bit is set (the net's lower bound
+// at least the skip threshold)?  Positions outside the grid never are.
 __device__ __forceinline__ bool prop_skippable(const PropGrid &pg, V3 P)
 {
     const float nf = (float)pg.n;
@@ -979,52 +982,55 @@ __device__ __forceinline__ bool prop_skippable(const PropGrid &pg, V3 P)
     const float fy = (P.y - pg.lo[1]) * pg.scale[1];
     const float fz = (P.z - pg.lo[2]) * pg.scale[2];
     if (!(fx >= 0.0f && fx < nf && fy >= 0.0f && fy < nf && fz >= 0.0f && fz < nf)) return false;
-    const uint32_t ix = (uint32_t)fx, iy = (uint32_t)fy, iz = (uint32_t)fz;   // each < n
-    return __ldg(pg.grid + ((size_t)iz * pg.n + iy) * pg.n + ix) >= pg.tau;
+    const uint32_t c = ((uint32_t)fz * pg.n + (uint32_t)fy) * pg.n + (uint32_t)fx;   // each index < n
+    return (pg.bits[c >> 5] >> (c & 31u)) & 1u;
 }
 
-// After a march step (the ray at its next position P, index nm + 1): skip
-// the run of skippable positions that starts there -- at most pg.run, and
-// never the last position before t1 or the sample cap -- by taking exactly
-// the steps ray_advance takes after a sample above the threshold, so every
-// later position is bit-identical to the exact march's.  The ray then waits
-// at the position after the run, whose sample confirms it (ray_advance).
-// Counts: the skipped positions are in nm and ns.
+// k march steps from P, as ray_advance takes them (fixed step length)
+__device__ __forceinline__ V3 prop_steps(V3 P, V3 V, float dt, uint32_t k)
+{
+    for (uint32_t j = 0; j < k; j++) P = P + V * dt;
+    return P;
+}
+
+// After a march step (the ray at its next position P, index nm + 1): the
+// run of skippable positions that starts there -- at most pg.run, never the
+// last position before t1 or the sample cap.  The ray stays at P; its
+// pending sample is the position after the run, which confirms it
+// (ray_advance<true>), and ray_sample_point<true> finds it by taking the
+// run's steps exactly as the march would, so every later position is
+// bit-identical to the exact march's.
 __device__ __forceinline__ void prop_form_run(Ray &r, const PropGrid &pg)
 {
     if (r.nm < r.pnoskip) return;
     uint32_t k = 0;
     V3 Q = r.P;
-    float tq = r.t, tpq = r.tprev;
+    float tq = r.t;
     while (k < pg.run && r.nm + k + 1 < r.cap && prop_skippable(pg, Q)) {
         const float tn = tq + r.dt;
         if (tn > r.t1) break;   // Q is the last position in the box: it confirms
-        tpq = tq;
         tq = tn;
         Q = Q + r.V * r.dt;
         k++;
     }
-    if (k) {
-        r.Ps = r.P;
-        r.ts = r.t;
-        r.tps = r.tprev;
-        r.P = Q;
-        r.t = tq;
-        r.tprev = tpq;
-        r.nm += k;
-        r.ns += k;
-        r.prun = k;
-    }
+    r.pst = (r.pst & ~63u) | k;
 }
 
-// The march position `offset` evaluated samples after the pending one at P
-// (index nm + 1), assuming every sample until then is above the threshold
-// and confirms its run: the positions ray_advance<true> and prop_form_run
-// visit.  valid = false once the ray would have left the box or the cap.
+// The march position `offset` evaluated samples after the pending one (run
+// `run` steps past P, index nm + run + 1), assuming every sample until then
+// is above the threshold and confirms its run: the positions
+// ray_advance<true> and prop_form_run visit.  valid = false once the ray
+// would have left the box or reached the cap.
 __device__ __forceinline__ V3 prop_march_ahead(V3 P, V3 V, float dt, float t, float t1, uint32_t nm, uint32_t cap,
-                                               uint32_t noskip, const PropGrid &pg, uint32_t offset, bool &valid)
+                                               uint32_t noskip, uint32_t run, const PropGrid &pg, uint32_t offset,
+                                               bool &valid)
 {
     valid = true;
+    for (uint32_t j = 0; j < run; j++) {
+        t = t + dt;
+        P = P + V * dt;
+    }
+    nm += run;
     for (uint32_t j = 0; j < offset; j++) {
         nm += 1;
         if (nm >= cap) {
@@ -1052,10 +1058,16 @@ __device__ __forceinline__ V3 prop_march_ahead(V3 P, V3 V, float dt, float t, fl
     return P;
 }
 
-// Where the next lambda sample of this ray is taken.
+// Where the next lambda sample of this ray is taken.  PROP: a pending
+// sample that confirms a run of the learned proposal lies the run's steps
+// past P.
+template <bool PROP = false>
 __device__ __forceinline__ V3 ray_sample_point(const Ray &r)
 {
     V3 Q = r.P;
+    if constexpr (PROP) {
+        if (r.phase <= PH_MARCH) return prop_steps(Q, r.V, r.dt, prop_run(r));
+    }
     if (r.phase >= PH_NORM0) {
         const uint32_t k = r.phase - PH_NORM0;   // kernel.cu:457-463
         const float m = r.mag;
@@ -1120,21 +1132,27 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
         }
     } else {
         if constexpr (PROP) {
-            if (r.prun) {
+            const uint32_t k = prop_run(r);
+            if (k) {
                 if (!(lam > pg->tau)) {
-                    // not clearly empty (NaN included): rewind the run
-                    r.P = r.Ps;
-                    r.t = r.ts;
-                    r.tprev = r.tps;
-                    r.nm -= r.prun;
-                    r.ns -= r.prun;
-                    r.pnoskip = r.nm + r.prun + 1;
-                    r.prun = 0;
-                    r.pgen += 1;
-                    r.prej += 1;
+                    // not clearly empty (NaN included): the ray, still at the
+                    // run's first position, evaluates every position through
+                    // this one exactly
+                    r.pnoskip = r.nm + k + 1;
+                    // run 0, rewind counter + 1 (mod 256), discarded samples + 1
+                    r.pst = (((r.pst >> 14) + 1u) << 14) | (((prop_gen(r) + 1u) & 255u) << 6);
                     return RAY_CONTINUE;
                 }
-                r.prun = 0;   // confirmed: the sample is the march sample at this position
+                // confirmed: the run's steps, as the exact march takes them;
+                // the sample is the march sample at the position after them
+                for (uint32_t j = 0; j < k; j++) {
+                    r.tprev = r.t;
+                    r.t = r.t + r.dt;
+                    r.P = r.P + r.V * r.dt;
+                }
+                r.nm += k;
+                r.ns += k;
+                r.pst &= ~63u;
             }
         }
         r.nm += 1;

@@ -40,6 +40,12 @@ RenderJob make_job(const LyapCam *cam, const LyapParams *prm, const int32_t *d_s
 // cached per device, net hash, n and dilation for the life of the process
 cudaError_t proposal_grid(const LyapNet &net, uint32_t n, uint32_t dilate, const float **grid,
                           unsigned long long *stats, cudaStream_t stream);
+// the march's form of it for one threshold: bit c set when cell c >= tau
+// (PropGrid.bits), cached likewise per threshold
+cudaError_t proposal_bits(const LyapNet &net, uint32_t n, uint32_t dilate, float tau, const uint32_t **bits,
+                          unsigned long long *stats, cudaStream_t stream);
+// shared memory the proposal's bits take in the render (0: they stay in global memory)
+uint32_t proposal_smem_bytes(const RenderJob &job);
 // LyapRenderExt.proposal when the struct has the field, else null (lyap_capi.cu)
 const LyapNet *ext_proposal(const LyapRenderExt *ext);
 

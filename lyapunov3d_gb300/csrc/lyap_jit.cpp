@@ -301,7 +301,9 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
                       unsigned long long *d_stats, uint32_t blocks_per_sm, uint32_t threads, cudaStream_t stream,
                       cudaError_t *launch_err, std::string *why)
 {
-    Entry *e = get_entry(h_seq, job.seq_period, job.prm.settle, why, job.prop.grid != nullptr);
+    const bool prop = job.prop.bits != nullptr;
+    const uint32_t smem = proposal_smem_bytes(job);
+    Entry *e = get_entry(h_seq, job.seq_period, job.prm.settle, why, prop);
     if (!e) return 0;
     const int sms = device_sm_count();
     if (sms <= 0) {
@@ -315,20 +317,20 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
         {
             std::lock_guard<std::mutex> lock(g_mu);
             int &cached = e->render_blocks_per_sm[mode & 1u][dev & 63];
-            if (!cached) {
+            if (!cached || smem) {
                 if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)e->render[mode], (int)threads,
-                                                                  0) != cudaSuccess || nb <= 0)
+                                                                  smem) != cudaSuccess || nb <= 0)
                     nb = jit_render_min_blocks(mode);
-                cached = nb;
+                if (!smem) cached = nb;
             }
-            nb = cached;
+            if (!smem) nb = cached;
         }
         blocks_per_sm = (uint32_t)nb;
     }
     const uint32_t grid = (uint32_t)sms * blocks_per_sm;
     RenderJob j = job;
     void *args[] = {&j, &d_work_counter, &d_stats};
-    *launch_err = cudaLaunchKernel((const void *)e->render[mode], dim3(grid), dim3(threads), args, 0, stream);
+    *launch_err = cudaLaunchKernel((const void *)e->render[mode], dim3(grid), dim3(threads), args, smem, stream);
     {
         std::lock_guard<std::mutex> lock(g_mu);
         g_launches++;

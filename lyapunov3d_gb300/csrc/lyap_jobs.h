@@ -7,17 +7,19 @@
 
 namespace lyapgb {
 
-// The learned proposal as the march reads it: a lower bound of the net's
-// lambda per cell of an n^3 grid over the net's box.  A march position whose
-// cell holds a value >= tau (opaque threshold + margin) may be skipped, at
-// most `run` positions in a row; the sample after every run is evaluated
-// exactly and confirms it (prop_form_run and ray_advance, lyap_device.cuh).
+// The learned proposal as the march reads it: one bit per cell of an n^3
+// grid over the net's box, set when the cell's lower bound of the net's
+// lambda is at least tau (opaque threshold + margin).  A march position in a
+// set cell may be skipped, at most `run` positions in a row; the sample
+// after every run is evaluated exactly and confirms it (prop_form_run and
+// ray_advance, lyap_device.cuh).
 struct PropGrid {
-    const float *grid;           // device, n^3 floats, x fastest; null = no proposal
+    const uint32_t *bits;        // device, n^3 bits, cell (x + (y + z n) n) = bit c % 32 of word c / 32; null = none
     uint32_t n;                  // cells per axis
     uint32_t run;                // longest run of skipped positions (segment length - 1)
     float lo[3], scale[3];       // cell coordinate = (P - lo) * scale
     float tau;                   // skip / confirm threshold
+    uint32_t smem_words;         // > 0: the render copies the bits into shared memory first
 };
 
 // One frame to render: everything kernel_calc_render receives (kernel.cu:500)

@@ -218,7 +218,7 @@ __device__ __forceinline__ void finish_pixel(RGBA *rgba, LyapPoint *points, uint
     }
     st.march += r.nm - r.ns;
     st.prop_skip += r.ns;
-    st.prop_rej += r.prej;
+    st.prop_rej += prop_rewound(r);
     st.hone += r.nh;
     st.normal += hit ? 6u : 0u;
     st.hits += hit ? 1u : 0u;
@@ -266,12 +266,12 @@ __device__ __forceinline__ bool known_ahead(const Ray &r, bool fixed_step)
 struct AheadState {
     V3 P, V, QdV;
     float dt, mag, t, t1;
-    uint32_t phase, nm, cap, noskip;
+    uint32_t phase, nm, cap, noskip, run;
 };
 
 __device__ __forceinline__ AheadState ahead_state(const Ray &r)
 {
-    return AheadState{r.P, r.V, r.QdV, r.dt, r.mag, r.t, r.t1, r.phase, r.nm, r.cap, r.pnoskip};
+    return AheadState{r.P, r.V, r.QdV, r.dt, r.mag, r.t, r.t1, r.phase, r.nm, r.cap, r.pnoskip, prop_run(r)};
 }
 
 // lane `src`'s AheadState (the march bookkeeping only with a proposal)
@@ -297,6 +297,7 @@ __device__ __forceinline__ AheadState shfl_ahead(const AheadState &a, uint32_t s
         o.nm = __shfl_sync(FULL, a.nm, src);
         o.cap = __shfl_sync(FULL, a.cap, src);
         o.noskip = __shfl_sync(FULL, a.noskip, src);
+        o.run = __shfl_sync(FULL, a.run, src);
     }
     return o;
 }
@@ -333,7 +334,7 @@ __device__ __forceinline__ V3 sample_ahead(const AheadState &a, const PropGrid &
 {
     if constexpr (PROP) {
         if (a.phase <= PH_MARCH)
-            return prop_march_ahead(a.P, a.V, a.dt, a.t, a.t1, a.nm, a.cap, a.noskip, pg, offset, valid);
+            return prop_march_ahead(a.P, a.V, a.dt, a.t, a.t1, a.nm, a.cap, a.noskip, a.run, pg, offset, valid);
     }
     return sample_ahead(a.P, a.V, a.dt, a.mag, a.QdV, a.phase, offset, valid);
 }
@@ -344,7 +345,7 @@ __device__ __forceinline__ V3 sample_ahead(const AheadState &a, const PropGrid &
 // the march back, and the samples taken ahead no longer continue it).
 __device__ __forceinline__ bool still_ahead(const Ray &r, uint32_t kind, float qdt0, uint32_t gen0)
 {
-    return kind == 1u ? (r.phase == PH_MARCH && r.pgen == gen0)
+    return kind == 1u ? (r.phase == PH_MARCH && prop_gen(r) == gen0)
                       : kind == 2u ? r.phase >= PH_NORM0 : (kind == 3u && r.phase == PH_HONE && r.Qdt == qdt0);
 }
 
@@ -395,7 +396,7 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
             }
         }
     }
-    V3 Q = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
+    V3 Q = active ? ray_sample_point<PROP>(r) : v3(3.0f, 3.0f, 3.0f);
     if (ne) {
         // every lane reads its owner's state (its own, for non-helpers)
         const AheadState o = shfl_ahead<PROP>(ahead_state(r), owner);
@@ -424,7 +425,7 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     if (active) {
         const uint32_t kind = sample_kind(r);   // 1: march, 2: normal, 3: hone
         const float qdt0 = r.Qdt;
-        const uint32_t gen0 = r.pgen;
+        const uint32_t gen0 = prop_gen(r);
         // this ray's helpers: ranks idx, idx + ne, ... below ni, one sample each
         uint32_t idx = 0, nh = 0;
         if (ne && ((emask >> lane) & 1u)) {
@@ -490,7 +491,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
             }
         }
     }
-    V3 Q0 = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
+    V3 Q0 = active ? ray_sample_point<PROP>(r) : v3(3.0f, 3.0f, 3.0f);
     V3 Q1 = v3(3.0f, 3.0f, 3.0f);
     if (ahead_self) {
         bool v;
@@ -525,7 +526,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     if (active) {
         const uint32_t kind = sample_kind(r);   // 1: march, 2: normal, 3: hone
         const float qdt0 = r.Qdt;
-        const uint32_t gen0 = r.pgen;
+        const uint32_t gen0 = prop_gen(r);
         // this ray's helpers: ranks idx, idx + ne, ... below ni, two samples each
         uint32_t idx = 0, nh = 0;
         if (ne && ahead) {
@@ -609,6 +610,16 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
     const bool fixed_step = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f);
     const bool spec_ok = fixed_step && !(job.flags & LYAP_FLAG_NO_SPECULATION);
     const bool bracket_mode = (job.flags & LYAP_FLAG_BISECT_F64) != 0u;
+    PropGrid pg = job.prop;
+    if constexpr (PROP) {
+        // the proposal's bits in shared memory when they fit (the launch sized it)
+        extern __shared__ uint32_t prop_bits[];
+        if (pg.smem_words) {
+            for (uint32_t i = threadIdx.x; i < pg.smem_words; i += blockDim.x) prop_bits[i] = __ldg(pg.bits + i);
+            __syncthreads();
+            pg.bits = prop_bits;
+        }
+    }
     LaneStats st = {};
     Ray r;
     r.phase = PH_MARCH0;
@@ -639,7 +650,6 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
                         active = true;
                     } else {
                         r.nm = r.nh = r.ns = 0;
-                        r.prej = 0;
                         finish_pixel(job.rgba, job.points, job.counts, my, r, false, cr.C, job.lights,
                                      job.n_lights, job.light_model, st);
                     }
@@ -655,10 +665,9 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
 
         int res;
         if constexpr (RenderTuning<Lam>::pairs)
-            res = sample_round_pair<PROP>(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, job.prop,
-                                          st);
+            res = sample_round_pair<PROP>(r, active, amask, lam, job.prm, fixed_step, spec_ok, bracket_mode, pg, st);
         else
-            res = sample_round<PROP>(r, active, amask, lam, job.prm, spec_ok, bracket_mode, job.prop, st);
+            res = sample_round<PROP>(r, active, amask, lam, job.prm, spec_ok, bracket_mode, pg, st);
         if (active && res == RAY_BRACKET) {
             // precision form: hand the crossing to the FP64 bisection pass
             job.bracket[2 * (size_t)pix + 0] = r.tprev;
@@ -676,7 +685,7 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
             }
             st.march += r.nm - r.ns;
             st.prop_skip += r.ns;
-            st.prop_rej += r.prej;
+            st.prop_rej += prop_rewound(r);
             st.rays += 1;
             active = false;
         } else if (active && res != RAY_CONTINUE) {

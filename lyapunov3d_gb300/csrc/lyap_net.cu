@@ -543,6 +543,22 @@ __global__ void __launch_bounds__(256) grid_cells(const float *__restrict__ corn
     }
 }
 
+// the proposal's bits for one threshold: bit c set when cell[c] >= tau
+__global__ void __launch_bounds__(256) grid_bits(const float *__restrict__ cell, uint32_t *__restrict__ bits,
+                                                 uint64_t ncell, float tau)
+{
+    const uint64_t nword = (ncell + 31) / 32;
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nword;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t b = 0;
+        for (uint32_t j = 0; j < 32; j++) {
+            const uint64_t c = w * 32 + j;
+            if (c < ncell && cell[c] >= tau) b |= 1u << j;
+        }
+        bits[w] = b;
+    }
+}
+
 // the minimum over the (up to) 27 cells around each cell
 __global__ void __launch_bounds__(256) grid_dilate(const float *__restrict__ in, float *__restrict__ out, uint32_t n)
 {
@@ -620,18 +636,79 @@ std::mutex g_grid_mu;
 std::map<std::tuple<int, uint64_t, uint32_t, uint32_t>, GridEntry> g_grids;
 uint64_t g_grid_order = 0;
 constexpr size_t kGridsKeep = 8;
+// the bits of a grid for one threshold (tau's bit pattern in the key)
+std::map<std::tuple<int, uint64_t, uint32_t, uint32_t, uint32_t>, GridEntry> g_bits;
+
+template <class Map>
+void drop_oldest(Map &m)
+{
+    if (m.size() < kGridsKeep) return;
+    auto old = m.begin();
+    for (auto jt = m.begin(); jt != m.end(); ++jt)
+        if (jt->second.order < old->second.order) old = jt;
+    cudaFree(old->second.grid);   // synchronises the device: no launch still reads it
+    m.erase(old);
+}
 
 }  // namespace
 
+static cudaError_t proposal_grid_locked(const LyapNet &netw, uint64_t hash, uint32_t n, uint32_t dilate,
+                                       const float **grid, unsigned long long *stats, cudaStream_t s);
+
 cudaError_t proposal_grid(const LyapNet &netw, uint32_t n, uint32_t dilate, const float **grid,
                           unsigned long long *stats, cudaStream_t s)
+{
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    return proposal_grid_locked(netw, fnv64(&netw, offsetof(LyapNet, hash)), n, dilate, grid, stats, s);
+}
+
+cudaError_t proposal_bits(const LyapNet &netw, uint32_t n, uint32_t dilate, float tau, const uint32_t **bits,
+                          unsigned long long *stats, cudaStream_t s)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    uint32_t tau_bits;
+    memcpy(&tau_bits, &tau, sizeof(tau_bits));
+    const uint64_t hash = fnv64(&netw, offsetof(LyapNet, hash));
+    const auto key = std::make_tuple(dev, hash, n, dilate, tau_bits);
+    std::lock_guard<std::mutex> lock(g_grid_mu);
+    auto it = g_bits.find(key);
+    if (it != g_bits.end()) {
+        it->second.order = ++g_grid_order;
+        *bits = reinterpret_cast<const uint32_t *>(it->second.grid);
+        return cudaSuccess;
+    }
+    const float *grid = nullptr;
+    if ((e = proposal_grid_locked(netw, hash, n, dilate, &grid, stats, s)) != cudaSuccess) return e;
+    const uint64_t ncell = (uint64_t)n * n * n, nword = (ncell + 31) / 32;
+    uint32_t *out = nullptr;
+    if ((e = cudaMalloc((void **)&out, nword * sizeof(uint32_t))) != cudaSuccess) return e;
+    net::grid_bits<<<(uint32_t)device_sm_count() * 4u, 256, 0, s>>>(grid, out, ncell, tau);
+    e = cudaGetLastError();
+    // complete before any stream may read it from the cache
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaFree(out);
+        return e;
+    }
+    drop_oldest(g_bits);
+    GridEntry ent;
+    ent.grid = reinterpret_cast<float *>(out);
+    ent.order = ++g_grid_order;
+    g_bits[key] = ent;
+    *bits = out;
+    return cudaSuccess;
+}
+
+static cudaError_t proposal_grid_locked(const LyapNet &netw, uint64_t hash, uint32_t n, uint32_t dilate,
+                                       const float **grid, unsigned long long *stats, cudaStream_t s)
 {
     using namespace net;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    const auto key = std::make_tuple(dev, fnv64(&netw, offsetof(LyapNet, hash)), n, dilate);
-    std::lock_guard<std::mutex> lock(g_grid_mu);
+    const auto key = std::make_tuple(dev, hash, n, dilate);
     auto it = g_grids.find(key);
     if (it != g_grids.end()) {
         it->second.order = ++g_grid_order;
@@ -683,13 +760,7 @@ cudaError_t proposal_grid(const LyapNet &netw, uint32_t n, uint32_t dilate, cons
         cudaFree(out);
         return e;
     }
-    if (g_grids.size() >= kGridsKeep) {
-        auto old = g_grids.begin();
-        for (auto jt = g_grids.begin(); jt != g_grids.end(); ++jt)
-            if (jt->second.order < old->second.order) old = jt;
-        cudaFree(old->second.grid);   // synchronises the device: no launch still reads it
-        g_grids.erase(old);
-    }
+    drop_oldest(g_grids);
     GridEntry ent;
     ent.grid = out;
     ent.order = ++g_grid_order;

@@ -24,6 +24,11 @@ int device_sm_count()
     return cached[dev];
 }
 
+uint32_t proposal_smem_bytes(const RenderJob &job)
+{
+    return job.prop.bits ? job.prop.smem_words * 4u : 0u;
+}
+
 cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_counter,
                           unsigned long long *d_stats, uint32_t blocks_per_sm, uint32_t threads,
                           cudaStream_t stream)
@@ -33,16 +38,18 @@ cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_
     if (threads == 0) threads = LYAP_RENDER_THREADS;
     if (blocks_per_sm == 0) blocks_per_sm = LYAP_RENDER_MIN_BLOCKS;
     const uint32_t grid = (uint32_t)sms * blocks_per_sm;
-    const bool prop = job.prop.grid != nullptr;   // the learned proposal's instantiation
+    const bool prop = job.prop.bits != nullptr;   // the learned proposal's instantiation
+    const uint32_t smem = proposal_smem_bytes(job);
     if (mode == MODE_PRODUCT) {
         if (prop)
             render_persistent<RuntimeLambda<MODE_PRODUCT>, true>
-                <<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
+                <<<grid, threads, smem, stream>>>(job, d_work_counter, d_stats);
         else
             render_persistent<RuntimeLambda<MODE_PRODUCT>><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
     } else {
         if (prop)
-            render_persistent<RuntimeLambda<MODE_PLAIN>, true><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
+            render_persistent<RuntimeLambda<MODE_PLAIN>, true>
+                <<<grid, threads, smem, stream>>>(job, d_work_counter, d_stats);
         else
             render_persistent<RuntimeLambda<MODE_PLAIN>><<<grid, threads, 0, stream>>>(job, d_work_counter, d_stats);
     }
