@@ -973,8 +973,14 @@ __device__ __forceinline__ uint32_t prop_run(const Ray &r) { return r.pst & 63u;
 __device__ __forceinline__ uint32_t prop_gen(const Ray &r) { return (r.pst >> 6) & 255u; }
 __device__ __forceinline__ uint32_t prop_rewound(const Ray &r) { return r.pst >> 14; }
 
+// The proposal's bits in shared memory (the render's dynamic shared memory,
+// filled at its start when PropGrid.smem_words > 0).
+extern __shared__ uint32_t lyap_prop_smem[];
+
 // Is the march position P in a cell whose bit is set (the net's lower bound
-// at least the skip threshold)?  Positions outside the grid never are.
+// at least the skip threshold)?  Positions outside the grid never are.  pg
+// is the kernel parameter's copy (__grid_constant__): its fields are read
+// from the constant bank and hold no registers across the lambda loop.
 __device__ __forceinline__ bool prop_skippable(const PropGrid &pg, V3 P)
 {
     const float nf = (float)pg.n;
@@ -983,7 +989,8 @@ __device__ __forceinline__ bool prop_skippable(const PropGrid &pg, V3 P)
     const float fz = (P.z - pg.lo[2]) * pg.scale[2];
     if (!(fx >= 0.0f && fx < nf && fy >= 0.0f && fy < nf && fz >= 0.0f && fz < nf)) return false;
     const uint32_t c = ((uint32_t)fz * pg.n + (uint32_t)fy) * pg.n + (uint32_t)fx;   // each index < n
-    return (pg.bits[c >> 5] >> (c & 31u)) & 1u;
+    const uint32_t w = pg.smem_words ? lyap_prop_smem[c >> 5] : __ldg(pg.bits + (c >> 5));
+    return (w >> (c & 31u)) & 1u;
 }
 
 // k march steps from P, as ray_advance takes them (fixed step length)

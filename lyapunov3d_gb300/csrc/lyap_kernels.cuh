@@ -191,25 +191,31 @@ __device__ __forceinline__ void store_point(LyapPoint *dst, const Ray &r, bool h
     }
 }
 
+// The colour of a hit (shade, kernel.cu:25-106) as RGBA8.  Out of line and
+// by value: it runs once per ray, and kept out of the sample rounds' code it
+// leaves the instruction cache to the code that runs every round.
+static __device__ __noinline__ uint32_t shade_pixel(V3 P, V3 N, float a, float c, float l, V3 camC,
+                                                    const LyapLight *lights, uint32_t n_lights, uint32_t light_model)
+{
+    LyapPoint pt;
+    pt.P = LyapVec{P.x, P.y, P.z};
+    pt.N = LyapVec{N.x, N.y, N.z};
+    pt.a = a;
+    pt.c = c;
+    pt.l = l;
+    C4 col = (light_model == LYAP_LIGHT_DIRECTIONAL) ? shade_directional(pt, lights, n_lights)
+                                                     : shade_spot(pt, camC, lights, n_lights);
+    return (uint32_t)to_byte(col.x) | ((uint32_t)to_byte(col.y) << 8) | ((uint32_t)to_byte(col.z) << 16) |
+           ((uint32_t)to_byte(col.w) << 24);
+}
+
 // Write one finished pixel: point, colour, optional per-pixel sample counts.
 __device__ __forceinline__ void finish_pixel(RGBA *rgba, LyapPoint *points, uint32_t *counts, uint32_t ind,
                                              const Ray &r, bool hit, V3 camC, const LyapLight *lights,
                                              uint32_t n_lights, uint32_t light_model, LaneStats &st)
 {
     store_point(points + ind, r, hit);
-    uint32_t px = 0;
-    if (hit) {
-        LyapPoint pt;
-        pt.P = LyapVec{r.P.x, r.P.y, r.P.z};
-        pt.N = LyapVec{r.N.x, r.N.y, r.N.z};
-        pt.a = r.a;
-        pt.c = r.c;
-        pt.l = r.l;
-        C4 col = (light_model == LYAP_LIGHT_DIRECTIONAL) ? shade_directional(pt, lights, n_lights)
-                                                         : shade_spot(pt, camC, lights, n_lights);
-        px = (uint32_t)to_byte(col.x) | ((uint32_t)to_byte(col.y) << 8) | ((uint32_t)to_byte(col.z) << 16) |
-             ((uint32_t)to_byte(col.w) << 24);
-    }
+    const uint32_t px = hit ? shade_pixel(r.P, r.N, r.a, r.c, r.l, camC, lights, n_lights, light_model) : 0u;
     reinterpret_cast<uint32_t *>(rgba)[ind] = px;
     if (counts) {
         counts[3 * (size_t)ind + 0] = r.nm - r.ns;
@@ -610,14 +616,12 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
     const bool fixed_step = (job.prm.jitter == 0.0f) && (job.prm.nearMultiplier == 1.0f);
     const bool spec_ok = fixed_step && !(job.flags & LYAP_FLAG_NO_SPECULATION);
     const bool bracket_mode = (job.flags & LYAP_FLAG_BISECT_F64) != 0u;
-    PropGrid pg = job.prop;
+    const PropGrid &pg = job.prop;   // the parameter itself: constant-bank reads
     if constexpr (PROP) {
         // the proposal's bits in shared memory when they fit (the launch sized it)
-        extern __shared__ uint32_t prop_bits[];
         if (pg.smem_words) {
-            for (uint32_t i = threadIdx.x; i < pg.smem_words; i += blockDim.x) prop_bits[i] = __ldg(pg.bits + i);
+            for (uint32_t i = threadIdx.x; i < pg.smem_words; i += blockDim.x) lyap_prop_smem[i] = __ldg(pg.bits + i);
             __syncthreads();
-            pg.bits = prop_bits;
         }
     }
     LaneStats st = {};
