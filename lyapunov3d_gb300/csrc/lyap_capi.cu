@@ -280,15 +280,15 @@ int lyap_render(const LyapCam *cam, const LyapParams *prm, const int32_t *d_seq,
                                              npix * 2 * sizeof(float)
                                        : 256;
     const size_t list_off = (bisect_bytes + 255) & ~(size_t)255;
-    const size_t scratch = list_off + npix * sizeof(uint32_t);
+    const size_t scratch = list_off + npix * sizeof(RayEntry);
     uint32_t *d_counter = nullptr;
     cudaError_t e = scratch_alloc((void **)&d_counter, scratch, s);
     if (e != cudaSuccess) return cuda_error(e, "lyap_render: scratch allocation");
     e = cudaMemsetAsync(d_counter, 0, 2 * sizeof(uint32_t), s);
-    job.list = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(d_counter) + list_off);
+    job.list = reinterpret_cast<RayEntry *>(reinterpret_cast<char *>(d_counter) + list_off);
     job.list_count = d_counter + 1;
     if (e == cudaSuccess)
-        e = launch_ray_list(job, const_cast<uint32_t *>(job.list), d_counter + 1, ext ? ext->d_stats : nullptr, s);
+        e = launch_ray_list(job, const_cast<RayEntry *>(job.list), d_counter + 1, ext ? ext->d_stats : nullptr, s);
     if (e == cudaSuccess && bisect) {
         char *base = reinterpret_cast<char *>(d_counter);
         job.hits = reinterpret_cast<uint32_t *>(base + 256);

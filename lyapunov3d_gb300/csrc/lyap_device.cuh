@@ -899,11 +899,13 @@ __device__ __forceinline__ CamRays cam_rays(const LyapCam &cam)
     return CamRays{v3(cam.C), v3(cam.S0), v3(cam.SDX), v3(cam.SDY), cam.M};
 }
 
-// Ray setup and box clipping (kernel.cu:160-315).  Returns false when the
-// ray misses the box [lMin, lMax]^3 (raymarch returns 1 before any sample).
-__device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapParams &prm, uint32_t sx, uint32_t sy)
+// Ray setup and box clipping (kernel.cu:160-315): the direction, where the
+// ray enters and leaves the box [lMin, lMax]^3, its step and its sample cap.
+// Returns false when the ray misses the box (raymarch returns 1 before any
+// sample).
+__device__ __forceinline__ bool ray_geometry(const CamRays &cam, const LyapParams &prm, uint32_t sx, uint32_t sy,
+                                             RayEntry &e)
 {
-    r.pst = r.pnoskip = 0;
     V3 V = (cam.S0 + cam.SDX * (float)sx) + cam.SDY * (float)sy;
     V = normalized(V);
     V = V / cam.M;
@@ -941,30 +943,56 @@ __device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapP
     }
     if (t0 < 0.0f) t0 = 0.0f;
 
-    r.V = V;
-    r.t = t0;
-    r.t1 = t1;
-    r.P = cam.C + V * t0;
-    r.a = 0.0f;
-    r.c = 0.0f;
     float Fdt;
     if (prm.stepMethod == 1)
         Fdt = (t1 - t0) / prm.depth;
     else
         Fdt = sqrtf(V.x * V.x + V.y * V.y + V.z * V.z) / prm.depth;
-    r.Fdt = Fdt;
-    r.dt = Fdt;
-    r.Ndt = Fdt / prm.nearMultiplier;
-    r.near = false;
-    float dmin = Fdt < r.Ndt ? Fdt : r.Ndt;
+    const float Ndt = Fdt / prm.nearMultiplier;
+    float dmin = Fdt < Ndt ? Fdt : Ndt;
     double capd = ceil((double)(t1 - t0) / (double)dmin * 1.001) + 16.0;
-    r.cap = (capd > 0.0 && capd < (double)MARCH_MAX) ? (uint32_t)capd : MARCH_MAX;
+    e.t0 = t0;
+    e.t1 = t1;
+    e.cap = (capd > 0.0 && capd < (double)MARCH_MAX) ? (uint32_t)capd : MARCH_MAX;
+    e.vx = V.x;
+    e.vy = V.y;
+    e.vz = V.z;
+    e.Fdt = Fdt;
+    return true;
+}
+
+// The ray's march state at its first sample, from its setup.
+__device__ __forceinline__ void ray_start(Ray &r, V3 C, const RayEntry &e, const LyapParams &prm)
+{
+    const V3 V = v3(e.vx, e.vy, e.vz);
+    r.pst = r.pnoskip = 0;
+    r.V = V;
+    r.t = e.t0;
+    r.t1 = e.t1;
+    r.P = C + V * e.t0;
+    r.a = 0.0f;
+    r.c = 0.0f;
+    r.Fdt = e.Fdt;
+    r.dt = e.Fdt;
+    r.Ndt = e.Fdt / prm.nearMultiplier;
+    r.near = false;
+    r.cap = e.cap;
     r.nm = 0;
     r.nh = 0;
     r.ns = 0;
     r.phase = PH_MARCH0;
     r.l = 0.0f;
-    r.tprev = t0;
+    r.tprev = e.t0;
+}
+
+// Ray setup and start in one (kernel.cu:160-315).  Returns false when the
+// ray misses the box.
+__device__ __forceinline__ bool ray_init(Ray &r, const CamRays &cam, const LyapParams &prm, uint32_t sx, uint32_t sy)
+{
+    r.pst = r.pnoskip = 0;
+    RayEntry e;
+    if (!ray_geometry(cam, prm, sx, sy, e)) return false;
+    ray_start(r, cam.C, e, prm);
     return true;
 }
 

@@ -16,7 +16,7 @@ cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_
                           cudaStream_t stream);
 // the render's pre-pass: finishes the pixels whose ray misses the box and
 // lists the others in `list` (length in *count, which must start at 0)
-cudaError_t launch_ray_list(const RenderJob &job, uint32_t *list, uint32_t *count, unsigned long long *d_stats,
+cudaError_t launch_ray_list(const RenderJob &job, RayEntry *list, uint32_t *count, unsigned long long *d_stats,
                             cudaStream_t stream);
 cudaError_t launch_bisect(const RenderJob &job, uint32_t mode, uint32_t halvings, unsigned long long *d_stats,
                           cudaStream_t stream);

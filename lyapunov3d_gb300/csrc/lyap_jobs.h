@@ -22,6 +22,18 @@ struct PropGrid {
     uint32_t smem_words;         // > 0: the render copies the bits into shared memory first
 };
 
+// A ray that meets the box, as the render's pre-pass (ray_list) lists it:
+// what ray_init derives for the march -- the direction, the box's entry and
+// exit (the slab test's FP64 divisions), the step and the sample cap (an FP64
+// division) -- so a lane of the render takes a new ray with two 16-byte loads
+// instead of repeating that setup.
+struct alignas(16) RayEntry {
+    uint32_t pix;
+    float t0, t1;
+    uint32_t cap;
+    float vx, vy, vz, Fdt;
+};
+
 // One frame to render: everything kernel_calc_render receives (kernel.cu:500)
 // plus the image size, the light model and optional outputs.
 struct RenderJob {
@@ -45,7 +57,7 @@ struct RenderJob {
     PropGrid prop;
     // the rays that meet the box, listed by ray_list (null: the queue runs
     // over every pixel); the render's queue hands out list[i]
-    const uint32_t *list;
+    const RayEntry *list;
     const uint32_t *list_count;  // device: entries in list
 };
 

@@ -647,15 +647,21 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
                     drained = true;
                 } else {
                     const uint32_t e = queue_entry(qi, nq, stride);
-                    const uint32_t my = job.list ? job.list[e] : e;
-                    pix = my;
-                    const uint32_t sx = my % job.width, sy = my / job.width;
-                    if (ray_init(r, cr, job.prm, sx, sy)) {
+                    if (job.list) {
+                        // a listed ray meets the box; its setup comes with it
+                        const RayEntry en = job.list[e];
+                        pix = en.pix;
+                        ray_start(r, cr.C, en, job.prm);
                         active = true;
                     } else {
-                        r.nm = r.nh = r.ns = 0;
-                        finish_pixel(job.rgba, job.points, job.counts, my, r, false, cr.C, job.lights,
-                                     job.n_lights, job.light_model, st);
+                        pix = e;
+                        if (ray_init(r, cr, job.prm, e % job.width, e / job.width)) {
+                            active = true;
+                        } else {
+                            r.nm = r.nh = r.ns = 0;
+                            finish_pixel(job.rgba, job.points, job.counts, e, r, false, cr.C, job.lights,
+                                         job.n_lights, job.light_model, st);
+                        }
                     }
                 }
             }

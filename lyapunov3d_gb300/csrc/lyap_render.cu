@@ -62,7 +62,7 @@ cudaError_t launch_render(const RenderJob &job, uint32_t mode, uint32_t *d_work_
 // pixel order within a block).  The render's queue then walks the list only:
 // handing out runs of missing rays one atomic at a time stalled every warp
 // of a frame with a sky band at the end of its scanline order.
-__global__ void __launch_bounds__(256) ray_list(const __grid_constant__ RenderJob job, uint32_t *__restrict__ list,
+__global__ void __launch_bounds__(256) ray_list(const __grid_constant__ RenderJob job, RayEntry *__restrict__ list,
                                                 uint32_t *__restrict__ count, unsigned long long *__restrict__ stats)
 {
     __shared__ uint32_t warp_n[8], block_base;
@@ -72,11 +72,14 @@ __global__ void __launch_bounds__(256) ray_list(const __grid_constant__ RenderJo
     LaneStats st = {};
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool cross = false;
+    RayEntry en;
     if (i < npix) {
         Ray r;
         r.phase = PH_MARCH0;
-        if (ray_init(r, cr, job.prm, i % job.width, i / job.width)) {
+        r.pst = 0;
+        if (ray_geometry(cr, job.prm, i % job.width, i / job.width, en)) {
             cross = true;
+            en.pix = i;
         } else {
             r.nm = r.nh = r.ns = 0;
             finish_pixel(job.rgba, job.points, job.counts, i, r, false, cr.C, job.lights, job.n_lights,
@@ -94,11 +97,11 @@ __global__ void __launch_bounds__(256) ray_list(const __grid_constant__ RenderJo
     __syncthreads();
     uint32_t off = block_base;
     for (uint32_t w = 0; w < warp; w++) off += warp_n[w];
-    if (cross) list[off + __popc(m & ((1u << lane) - 1u))] = i;
+    if (cross) list[off + __popc(m & ((1u << lane) - 1u))] = en;
     flush_stats(stats, st, FULL);
 }
 
-cudaError_t launch_ray_list(const RenderJob &job, uint32_t *list, uint32_t *count, unsigned long long *d_stats,
+cudaError_t launch_ray_list(const RenderJob &job, RayEntry *list, uint32_t *count, unsigned long long *d_stats,
                             cudaStream_t stream)
 {
     const uint64_t npix = (uint64_t)job.width * job.height;
