@@ -703,13 +703,22 @@ def run_batch_report(args):
         times.append(e0.elapsed_time(e1))
     info = db.batch.info()
     ms = statistics.mean(times)
+    db.d_stats.zero_()
+    db.run(stream)
+    torch.cuda.synchronize()
+    st = db.stats()
     print(json.dumps({
         "report": "batch", "requests": len(wls), "pixels": sum(w.width * w.height for w in wls),
         "scale": args.batch_scale, "create_s": t_create, "ms_per_launch": ms, "launch_ms": times,
         "plain_iters_per_launch": iters, "g_iters_per_s": iters / (ms * 1e-3) / 1e9,
         "tuned": {"tile": [info.tile_w, info.tile_h], "tiles_per_chunk": info.tiles_per_chunk,
                   "blocks_per_sm": info.blocks_per_sm, "candidates_ms": list(info.tuned_ms)[:info.candidates]},
-        "chunks": info.chunks}), flush=True)
+        "chunks": info.chunks,
+        "one_launch": {"samples": int(st[capi.STAT_SAMPLES]), "rays": int(st[capi.STAT_RAYS]),
+                       "rounds": int(st[capi.STAT_ROUNDS]),
+                       "lane_utilisation": float(st[capi.STAT_LANE_ROUNDS]) / max(1.0, 32.0 * float(st[capi.STAT_ROUNDS])),
+                       "max_rounds_one_warp": int(st[capi.STAT_MAX_ROUNDS]),
+                       "speculative_used": int(st[capi.STAT_SPEC_USED])}}), flush=True)
 
 
 def run_proposal_report(args):
