@@ -42,8 +42,9 @@ L2_FLUSH_BYTES = 512 << 20   # > 129 MB of L2
 # DRAM bytes (read + write) of one launch of the chosen render on the default
 # frame (1920x1080, seed 1), from one ncu capture of that kernel on that frame
 # (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass, mean of 2 launches):
-# the outputs (40 B per pixel) stay in L2 at kernel end
-RENDER_DRAM_BYTES_FRAME1080 = 4575232 + 551296
+# the listed rays' setup (32 B per ray, 66 MB) and the outputs (40 B per
+# pixel) mostly stay in L2
+RENDER_DRAM_BYTES_FRAME1080 = 20285440 + 598656
 
 
 def parse_args():
