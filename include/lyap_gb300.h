@@ -235,7 +235,9 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
                                           proposal's threshold, each of which sent
                                           its ray back to the start of the skipped
                                           run (evaluated, then discarded) */
-#define LYAP_STAT_COUNT    20
+#define LYAP_STAT_TAIL_HANDOVERS 20   /* render: rays a warp handed to another warp of
+                                          its block after the pixel queue drained */
+#define LYAP_STAT_COUNT    21
 
 /* LyapRenderExt / LyapVolumeExt flags.  Given the host copy of the sequence
  * (h_seq), the library compiles the kernels for that sequence at run time
@@ -246,6 +248,10 @@ LYAP_STATIC_ASSERT(sizeof(LyapPointD) == 72, "LyapPointD size");
 #define LYAP_FLAG_REQUIRE_JIT 2u  /* fail (LYAP_ERR_JIT) instead of falling back */
 #define LYAP_FLAG_NO_SPECULATION 4u /* render: idle lanes do not take samples
                                        ahead for running rays (same results) */
+#define LYAP_FLAG_NO_TAIL_BALANCE 32u /* render: after the pixel queue
+                                         drains, warps of a block do not hand
+                                         their longest rays to warps left
+                                         without one (same results) */
 #define LYAP_FLAG_SPREAD_ORDER 16u /* render: the pixel queue spreads
                                       consecutive pixels over the image
                                       instead of scanline order (same

@@ -29,6 +29,7 @@ LYAP_ERR_JIT = -7
 FLAG_NO_JIT = 1
 FLAG_REQUIRE_JIT = 2
 FLAG_NO_SPECULATION = 4
+FLAG_NO_TAIL_BALANCE = 32
 FLAG_BISECT_F64 = 8
 FLAG_SPREAD_ORDER = 16
 FORM_F64 = 2
@@ -42,8 +43,8 @@ MAX_LIGHTS = 16
 
 (STAT_SAMPLES, STAT_SKIPPED, STAT_MARCH, STAT_HONE, STAT_NORMAL, STAT_HITS, STAT_RAYS, STAT_FALLBACK, STAT_SPEC,
  STAT_SPEC_USED, STAT_ROUNDS, STAT_LANE_ROUNDS, STAT_MAX_ROUNDS, STAT_PROPOSAL_SKIPPED, STAT_PROPOSAL_POINTS,
- STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END, STAT_PROPOSAL_REWOUND) = range(20)
-STAT_COUNT = 20
+ STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END, STAT_PROPOSAL_REWOUND, STAT_TAIL_HANDOVERS) = range(21)
+STAT_COUNT = 21
 PROPOSAL_GRID_DEFAULT = 64
 # the proposal margin the library's users are pointed to: the smallest of the
 # measured margins at which the 1080p bench frame keeps >= 99.9 % of its

@@ -150,6 +150,7 @@ struct LaneStats {
     uint32_t rounds, lane_rounds;   // per warp, kept by every lane alike
     uint32_t prop_skip;             // march samples skipped on the learned proposal's word
     uint32_t prop_rej;              // samples a rewind of the proposal discarded
+    uint32_t handed;                // rays handed to another warp at the end of a frame
 };
 
 // position of the n-th (0-based) set bit of mask; mask has more than n bits
@@ -247,6 +248,8 @@ __device__ __forceinline__ void flush_stats(unsigned long long *stats, const Lan
     if (lane == leader && ps) atomicAdd(stats + LYAP_STAT_PROPOSAL_SKIPPED, (unsigned long long)ps);
     const uint32_t pr = __reduce_add_sync(mask, st.prop_rej);
     if (lane == leader && pr) atomicAdd(stats + LYAP_STAT_PROPOSAL_REWOUND, (unsigned long long)pr);
+    const uint32_t ho = __reduce_add_sync(mask, st.handed);
+    if (lane == leader && ho) atomicAdd(stats + LYAP_STAT_TAIL_HANDOVERS, (unsigned long long)ho);
     if (lane == leader && st.rounds) {
         atomicAdd(stats + LYAP_STAT_ROUNDS, (unsigned long long)st.rounds);
         atomicAdd(stats + LYAP_STAT_LANE_ROUNDS, (unsigned long long)st.lane_rounds);
@@ -591,6 +594,101 @@ __device__ __forceinline__ uint32_t queue_entry(uint32_t qi, uint32_t n, uint32_
     return stride ? (uint32_t)(((uint64_t)qi * stride) % n) : qi;
 }
 
+// ---------------------------------------------------- the end of a frame
+// After the pixel queue drains, warps leave as their rays end, and the few
+// long rays left run on fewer and fewer warps.  Within a block, a warp left
+// without rays asks for one, and a warp still holding two or more running
+// rays hands its longest over through a one-ray mailbox in shared memory;
+// the receiving warp runs it with 31 idle lanes sampling ahead for it.  The
+// whole ray state moves, so the ray continues exactly as it would have.
+// Only the warps of one block take part (always co-resident); no warp ever
+// waits for another's work, and the receivers' polling is bounded.
+struct TailBox {
+    Ray r;
+    uint32_t pix;
+    int state;   // TAIL_EMPTY, TAIL_WRITING, TAIL_FULL, TAIL_TAKING
+    int waiting, live, closed;   // warps asking / warps not yet gone / no more hand-overs
+};
+constexpr int TAIL_EMPTY = 0, TAIL_WRITING = 1, TAIL_FULL = 2, TAIL_TAKING = 3;
+constexpr uint32_t TAIL_POLLS = 1u << 20;        // a receiver's polls before it stops asking
+constexpr uint32_t TAIL_MIN_STEPS = 16u;         // rays with fewer march steps left stay put
+
+__device__ __forceinline__ int tail_load(const int *p) { return *(volatile const int *)p; }
+
+// A ray's march steps left (0 outside the march): what a hand-over is worth.
+__device__ __forceinline__ uint32_t tail_steps_left(const Ray &r)
+{
+    if (r.phase > PH_MARCH || !(r.dt > 0.0f)) return 0u;
+    const float k = (r.t1 - r.t) / r.dt;
+    return k >= 1.0e6f ? 1000000u : (k > 0.0f ? (uint32_t)k : 0u);
+}
+
+// A warp without rays (the queue drained): wait for a handed-over ray.
+// Returns true with the ray in lane 0's r / pix; false when no warp of the
+// block can hand one over any more (the warp then leaves).
+__device__ __forceinline__ bool tail_receive(TailBox &box, Ray &r, uint32_t &pix)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    int got = 0;
+    if (lane == 0) {
+        atomicAdd(&box.waiting, 1);
+        for (uint32_t it = 0; it < TAIL_POLLS; it++) {
+            if (atomicCAS(&box.state, TAIL_FULL, TAIL_TAKING) == TAIL_FULL) {
+                got = 1;
+                break;
+            }
+            // every warp still here is asking: nobody holds a ray to hand over
+            if (tail_load(&box.waiting) >= tail_load(&box.live)) break;
+            __nanosleep(256);
+        }
+        if (!got && tail_load(&box.waiting) < tail_load(&box.live)) {
+            // polls ran out: stop hand-overs, and take one already under way
+            atomicExch(&box.closed, 1);
+            __threadfence_block();
+            for (uint32_t it = 0; it < 65536u && tail_load(&box.state) == TAIL_WRITING; it++) __nanosleep(64);
+            if (atomicCAS(&box.state, TAIL_FULL, TAIL_TAKING) == TAIL_FULL) got = 1;
+        }
+        if (got) {
+            __threadfence_block();
+            r = box.r;
+            pix = box.pix;
+            __threadfence_block();
+            atomicExch(&box.state, TAIL_EMPTY);
+        } else {
+            atomicSub(&box.live, 1);   // leaving
+        }
+        atomicSub(&box.waiting, 1);
+    }
+    return __shfl_sync(FULL, got, 0) != 0;
+}
+
+// A warp in the tail with two or more running rays: hand the longest over
+// when a warp of the block is asking.  Returns true on the lane whose ray left.
+__device__ __forceinline__ bool tail_offer(TailBox &box, const Ray &r, uint32_t pix, bool active)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t amask = __ballot_sync(FULL, active);
+    if (__popc(amask) < 2) return false;
+    if (tail_load(&box.waiting) <= 0 || tail_load(&box.closed) || tail_load(&box.state) != TAIL_EMPTY) return false;
+    const uint32_t key = active ? tail_steps_left(r) : 0u;
+    const uint32_t best = __reduce_max_sync(FULL, key);
+    if (best < TAIL_MIN_STEPS) return false;
+    const uint32_t donor = __ffs(__ballot_sync(FULL, key == best)) - 1;
+    int gave = 0;
+    if (lane == donor && atomicCAS(&box.state, TAIL_EMPTY, TAIL_WRITING) == TAIL_EMPTY) {
+        if (tail_load(&box.closed)) {
+            atomicExch(&box.state, TAIL_EMPTY);
+        } else {
+            box.r = r;
+            box.pix = pix;
+            __threadfence_block();
+            atomicExch(&box.state, TAIL_FULL);
+            gave = 1;
+        }
+    }
+    return gave != 0;
+}
+
 template <class Lam>
 struct RenderTuning {
     static constexpr bool product = Lam::mode == MODE_PRODUCT;
@@ -630,6 +728,15 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
     uint32_t pix = 0;
     bool active = false, drained = false, drain_seen = false;
     if (stats && lane == 0) atomicMax(stats + LYAP_STAT_T_START, ~global_ns());
+    __shared__ TailBox tail_box;
+    const bool tail_balance = !(job.flags & LYAP_FLAG_NO_TAIL_BALANCE);
+    if (threadIdx.x == 0) {
+        tail_box.state = TAIL_EMPTY;
+        tail_box.waiting = 0;
+        tail_box.live = (int)(blockDim.x >> 5);
+        tail_box.closed = 0;
+    }
+    __syncthreads();
 
     for (;;) {
         // refill the lanes whose ray has ended
@@ -666,12 +773,24 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
                 }
             }
         }
-        const uint32_t amask = __ballot_sync(FULL, active);
-        if (stats && !drain_seen && __any_sync(FULL, drained)) {
+        if (!drain_seen && __any_sync(FULL, drained)) {
             drain_seen = true;
-            if (lane == 0) atomicMax(stats + LYAP_STAT_T_DRAIN, ~global_ns());
+            if (stats && lane == 0) atomicMax(stats + LYAP_STAT_T_DRAIN, ~global_ns());
         }
-        if (amask == 0) break;
+        // in the tail, hand the warp's longest ray to a warp of the block that asks
+        if (tail_balance && drain_seen && tail_offer(tail_box, r, pix, active)) {
+            active = false;
+            st.handed += 1;
+        }
+        const uint32_t amask = __ballot_sync(FULL, active);
+        if (amask == 0) {
+            // the queue has drained for every lane: take over a ray of another warp, or leave
+            if (tail_balance && tail_receive(tail_box, r, pix)) {
+                active = lane == 0;
+                continue;
+            }
+            break;
+        }
 
         int res;
         if constexpr (RenderTuning<Lam>::pairs)

@@ -219,3 +219,27 @@ def test_hone_cap_rays_vs_oracle(dev, oracle, frame_wl, flags):
         assert rc == 0 and not np.isnan(g["a"])
         assert np.array_equal(np.array(g["P"]), np.array([pt.P.x, pt.P.y, pt.P.z], dtype=np.float32))
         assert abs(float(g["l"]) - pt.l) <= LAM_TOL[ORC_PRODUCT] or (np.isnan(g["l"]) and np.isnan(pt.l))
+
+
+@pytest.mark.parametrize("jit,jitter", [(True, 0.0), (False, 0.0), (True, 0.5)])
+def test_tail_handover_gives_the_same_frame(dev, jit, jitter):
+    """After the pixel queue drains, warps hand their longest rays to warps
+    of the block left without one (the whole ray state moves).  The frame is
+    bit-identical to the render without hand-overs, which do happen."""
+    wl = scenes.full_render(1, 960, 540)
+    wl.params.jitter = jitter
+    f = DeviceFrame(wl, device=dev, counts=True)
+    f.run(capi.VARIANT_PRODUCT, jit=jit, flags=capi.FLAG_NO_TAIL_BALANCE)
+    torch.cuda.synchronize()
+    want = (f.d_rgba.clone(), f.d_points.clone(), f.d_counts.clone())
+    assert f.stats()[capi.STAT_TAIL_HANDOVERS] == 0
+    f.reset_stats()
+    f.d_points.fill_(0.0)
+    f.run(capi.VARIANT_PRODUCT, jit=jit)
+    torch.cuda.synchronize()
+    st = f.stats()
+    assert st[capi.STAT_TAIL_HANDOVERS] > 0
+    assert st[capi.STAT_RAYS] == wl.width * wl.height
+    assert torch.equal(f.d_rgba, want[0])
+    assert torch.equal(f.d_points.view(torch.int32), want[1].view(torch.int32))
+    assert torch.equal(f.d_counts, want[2])
