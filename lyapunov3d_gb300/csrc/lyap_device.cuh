@@ -1121,6 +1121,11 @@ __device__ __forceinline__ V3 ray_sample_point(const Ray &r)
 // in FP64 afterwards).
 enum : int { RAY_CONTINUE = 0, RAY_HIT = 1, RAY_MISS = 2, RAY_BRACKET = 3 };
 
+// The normal's normalisation at a ray's end (vec3.hpp:127-154), out of line:
+// it runs once per hit, and kept out of ray_advance's inlined copies it
+// leaves the instruction cache to the code every sample round runs.
+static __device__ __noinline__ V3 normalized_cold(V3 a) { return normalized(a); }
+
 // Feed one lambda sample to the ray (kernel.cu:318-473); the ray either asks
 // for its next sample (RAY_CONTINUE) or ends.  PROP: the learned proposal's
 // skipping (prop_form_run) after every march step, and the confirmation of
@@ -1146,7 +1151,7 @@ __device__ __forceinline__ int ray_advance(Ray &r, float lam, const LyapParams &
             else r.N.z = diff;
         }
         if (k == 5) {
-            r.N = normalized(r.N);
+            r.N = normalized_cold(r.N);
             return RAY_HIT;
         }
         r.phase += 1;
