@@ -70,6 +70,8 @@ def parse_args():
     ap.add_argument("--report", choices=["precision", "batch", "proposal"], default=None,
                     help="instead of the benchmark, print the precision form's error report or time the batch")
     ap.add_argument("--batch-scale", type=int, default=1, help="--report batch: divide every image side by this")
+    ap.add_argument("--batch-seq", default=None,
+                    help="--report batch: every request takes this sequence (the frames of one field)")
     return ap.parse_args()
 
 
@@ -686,7 +688,7 @@ def run_batch_report(args):
     from lyapunov3d_gb300 import capi, scenes
     from lyapunov3d_gb300.device import DeviceBatch
     dev = torch.device("cuda", 0)
-    wls = scenes.batch_workloads(seed=4, scale=args.batch_scale)
+    wls = scenes.batch_workloads(seed=4, scale=args.batch_scale, one_seq=args.batch_seq)
     t0 = time.perf_counter()
     db = DeviceBatch(wls, device=dev, variant=capi.VARIANT_PRODUCT, autotune=True, counts=True)
     t_create = time.perf_counter() - t0
@@ -710,7 +712,8 @@ def run_batch_report(args):
     st = db.stats()
     print(json.dumps({
         "report": "batch", "requests": len(wls), "pixels": sum(w.width * w.height for w in wls),
-        "scale": args.batch_scale, "create_s": t_create, "ms_per_launch": ms, "launch_ms": times,
+        "scale": args.batch_scale, "one_sequence": args.batch_seq, "specialised": int(info.specialised),
+        "create_s": t_create, "ms_per_launch": ms, "launch_ms": times,
         "plain_iters_per_launch": iters, "g_iters_per_s": iters / (ms * 1e-3) / 1e9,
         "tuned": {"tile": [info.tile_w, info.tile_h], "tiles_per_chunk": info.tiles_per_chunk,
                   "blocks_per_sm": info.blocks_per_sm, "candidates_ms": list(info.tuned_ms)[:info.candidates]},

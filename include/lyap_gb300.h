@@ -453,14 +453,17 @@ typedef struct {
     uint32_t variant;             /* LYAP_VARIANT_* for every request */
     uint32_t autotune;            /* 1: time the candidate launch shapes */
     uint32_t tile_w, tile_h, tiles_per_chunk, blocks_per_sm;   /* used when autotune = 0 */
-    uint32_t pad_;
+    uint32_t flags;               /* LYAP_FLAG_NO_JIT: never the kernel compiled for a
+                                     batch whose requests share one sequence */
     unsigned long long *d_stats;  /* optional device LYAP_STAT_COUNT array */
 } LyapBatchOptions;
 
 typedef struct {
     uint32_t size, requests, chunks;
     uint32_t tile_w, tile_h, tiles_per_chunk, blocks_per_sm, threads_per_block;
-    uint32_t candidates, pad_;
+    uint32_t candidates;
+    uint32_t specialised;         /* 1: every request has the same sequence, and the
+                                     batch runs the kernel compiled for it at run time */
     float tuned_ms[16];           /* time of each candidate on the sample */
 } LyapBatchInfo;
 

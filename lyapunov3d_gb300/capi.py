@@ -116,7 +116,7 @@ assert ctypes.sizeof(LyapRequest) == 352
 class LyapBatchOptions(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("variant", c_uint32), ("autotune", c_uint32), ("tile_w", c_uint32),
                 ("tile_h", c_uint32), ("tiles_per_chunk", c_uint32), ("blocks_per_sm", c_uint32),
-                ("pad_", c_uint32), ("d_stats", c_void_p)]
+                ("flags", c_uint32), ("d_stats", c_void_p)]
 
     def __init__(self, **kw):
         super().__init__()
@@ -128,7 +128,7 @@ class LyapBatchOptions(ctypes.Structure):
 class LyapBatchInfo(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("requests", c_uint32), ("chunks", c_uint32), ("tile_w", c_uint32),
                 ("tile_h", c_uint32), ("tiles_per_chunk", c_uint32), ("blocks_per_sm", c_uint32),
-                ("threads_per_block", c_uint32), ("candidates", c_uint32), ("pad_", c_uint32),
+                ("threads_per_block", c_uint32), ("candidates", c_uint32), ("specialised", c_uint32),
                 ("tuned_ms", ctypes.c_float * 16)]
 
 

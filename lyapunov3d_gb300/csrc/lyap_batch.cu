@@ -11,7 +11,11 @@
 // A warp renders one request at a time (its lambda loop must be uniform), so
 // it continues with the next chunk while that belongs to the same request
 // and otherwise lets its rays run out -- idle lanes speculate for the rays
-// still running (sample_round) -- before switching.
+// still running (sample_round) -- before switching (render_batch,
+// lyap_kernels.cuh).  When every request has the same sequence (and settle
+// count mod its period) -- the frames of an animation of one field -- the
+// kernel is compiled for that sequence at run time (ConstLambda, paired
+// rounds; LYAP_FLAG_NO_JIT in the options keeps the library's kernel).
 //
 // Autotuner: the tile shape (32x1, 8x4, 16x16), the tiles per chunk (1, 4)
 // and the resident blocks per SM (3, 4) are timed on every 8th chunk of the
@@ -25,126 +29,13 @@
 #include <new>
 #include <vector>
 
+#include <string>
+
 #include "lyap_internal.h"
+#include "lyap_jit.h"
 #include "lyap_kernels.cuh"
 
 namespace lyapgb {
-
-struct BatchTables {
-    const RenderJob *jobs;
-    const uint32_t *chunk_job;    // per chunk: request index
-    const uint32_t *chunk_tile;   // per chunk: first tile within the request
-    uint32_t n_chunks;
-    uint32_t tile_w, tile_h, tiles_per_chunk;
-};
-
-template <uint32_t MODE>
-__global__ void __launch_bounds__(128, 4) render_batch(const __grid_constant__ BatchTables tb,
-                                                       uint32_t *__restrict__ chunk_counter,
-                                                       unsigned long long *__restrict__ stats)
-{
-    if (tb.n_chunks == 0) return;
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t tile_px = tb.tile_w * tb.tile_h;
-    const uint32_t slots_per_chunk = tb.tiles_per_chunk * tile_px;
-    LaneStats st = {};
-
-    // the warp's request (uniform)
-    uint32_t cur = tb.chunk_job[0];
-    const RenderJob *J = tb.jobs + cur;
-    RuntimeLambda<MODE> lam(J->seq, J->seq_period, J->prm);
-    LyapParams prm = J->prm;
-    CamRays cr = cam_rays(J->cam);
-    uint32_t W = J->width, H = J->height, tiles_x = (W + tb.tile_w - 1) / tb.tile_w;
-    uint32_t n_tiles = tiles_x * ((H + tb.tile_h - 1) / tb.tile_h);
-    bool spec_ok = (prm.jitter == 0.0f) && (prm.nearMultiplier == 1.0f) && !(J->flags & LYAP_FLAG_NO_SPECULATION);
-    bool have_job = false;
-    uint32_t tile0 = 0, slot_next = 0, slot_end = 0;
-    uint32_t pending = 0xffffffffu;   // a claimed chunk of another request
-    bool no_more = false;
-
-    Ray r;
-    r.phase = PH_MARCH0;
-    uint32_t pix = 0;
-    bool active = false;
-
-    for (;;) {
-        // refill idle lanes from the current chunk, claiming chunks of the same request
-        for (;;) {
-            const bool need = !active && have_job;
-            const uint32_t mask = __ballot_sync(FULL, need);
-            if (mask == 0) break;
-            if (slot_next >= slot_end) {
-                if (no_more || pending != 0xffffffffu) break;
-                uint32_t c = 0;
-                if (lane == 0) c = atomicAdd(chunk_counter, 1u);
-                c = __shfl_sync(FULL, c, 0);
-                if (c >= tb.n_chunks) {
-                    no_more = true;
-                    break;
-                }
-                if (tb.chunk_job[c] != cur) {
-                    pending = c;   // switch once this request's rays have run out
-                    break;
-                }
-                tile0 = tb.chunk_tile[c];
-                slot_next = 0;
-                slot_end = slots_per_chunk;
-            }
-            const uint32_t s = slot_next + __popc(mask & ((1u << lane) - 1u));
-            slot_next += __popc(mask);
-            if (need && s < slot_end) {
-                const uint32_t tile = tile0 + s / tile_px, within = s % tile_px;
-                const uint32_t x = (tile % tiles_x) * tb.tile_w + within % tb.tile_w;
-                const uint32_t y = (tile / tiles_x) * tb.tile_h + within / tb.tile_w;
-                if (tile < n_tiles && x < W && y < H) {
-                    pix = x + y * W;
-                    if (ray_init(r, cr, prm, x, y)) {
-                        active = true;
-                    } else {
-                        r.nm = r.nh = r.ns = 0;
-                        finish_pixel(J->rgba, J->points, J->counts, pix, r, false, cr.C, J->lights, J->n_lights,
-                                     J->light_model, st);
-                    }
-                }
-            }
-        }
-        const uint32_t amask = __ballot_sync(FULL, active);
-        if (amask == 0) {
-            // every ray of this warp has ended: move to the pending request, or claim one
-            uint32_t c = pending;
-            if (c == 0xffffffffu) {
-                if (no_more) break;
-                if (lane == 0) c = atomicAdd(chunk_counter, 1u);
-                c = __shfl_sync(FULL, c, 0);
-                if (c >= tb.n_chunks) break;
-            }
-            pending = 0xffffffffu;
-            cur = tb.chunk_job[c];
-            J = tb.jobs + cur;
-            lam = RuntimeLambda<MODE>(J->seq, J->seq_period, J->prm);
-            prm = J->prm;
-            cr = cam_rays(J->cam);
-            W = J->width;
-            H = J->height;
-            tiles_x = (W + tb.tile_w - 1) / tb.tile_w;
-            n_tiles = tiles_x * ((H + tb.tile_h - 1) / tb.tile_h);
-            spec_ok = (prm.jitter == 0.0f) && (prm.nearMultiplier == 1.0f) && !(J->flags & LYAP_FLAG_NO_SPECULATION);
-            have_job = true;
-            tile0 = tb.chunk_tile[c];
-            slot_next = 0;
-            slot_end = slots_per_chunk;
-            continue;
-        }
-        const int res = sample_round<false>(r, active, amask, lam, prm, spec_ok, false, PropGrid{}, st);
-        if (active && res != RAY_CONTINUE) {
-            finish_pixel(J->rgba, J->points, J->counts, pix, r, res == RAY_HIT, cr.C, J->lights, J->n_lights,
-                         J->light_model, st);
-            active = false;
-        }
-    }
-    flush_stats(stats, st, FULL);
-}
 
 }  // namespace lyapgb
 
@@ -162,6 +53,7 @@ struct LyapBatch {
     uint32_t tile_w = 16, tile_h = 16, tiles_per_chunk = 1, blocks_per_sm = 3, threads = 128;
     uint32_t *d_chunks = nullptr;   // chunk_job then chunk_tile
     uint32_t n_chunks = 0;
+    cudaKernel_t jit_kernel = nullptr;   // the kernel compiled for the batch's one sequence, if any
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     LyapBatchInfo info;
@@ -219,10 +111,15 @@ cudaError_t launch_batch(const LyapBatch &b, uint32_t tw, uint32_t th, uint32_t 
     cudaError_t e = cudaMemsetAsync(b.d_counter, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     const uint32_t grid = (uint32_t)sms * bps;
+    if (b.jit_kernel) {
+        uint32_t *counter = b.d_counter;
+        void *args[] = {&tb, &counter, &stats};
+        return cudaLaunchKernel((const void *)b.jit_kernel, dim3(grid), dim3(b.threads), args, 0, s);
+    }
     if (b.mode == MODE_PRODUCT)
-        render_batch<MODE_PRODUCT><<<grid, b.threads, 0, s>>>(tb, b.d_counter, stats);
+        render_batch<RuntimeLambda<MODE_PRODUCT>><<<grid, b.threads, 0, s>>>(tb, b.d_counter, stats);
     else
-        render_batch<MODE_PLAIN><<<grid, b.threads, 0, s>>>(tb, b.d_counter, stats);
+        render_batch<RuntimeLambda<MODE_PLAIN>><<<grid, b.threads, 0, s>>>(tb, b.d_counter, stats);
     return cudaGetLastError();
 }
 
@@ -289,6 +186,32 @@ int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOption
         if (s) cudaStreamDestroy(s);
         destroy(b);
         return cuda_error(e, "lyap_batch_create: device tables");
+    }
+    // one sequence for every request (same symbols, same settle count mod its
+    // period): the batch kernel compiled for it
+    if (!(opt && (opt->flags & LYAP_FLAG_NO_JIT))) {
+        std::vector<int32_t> first, cur;
+        bool same = true;
+        for (uint32_t i = 0; i < n && same && e == cudaSuccess; i++) {
+            cur.resize(reqs[i].seq_len);
+            e = cudaMemcpy(cur.data(), reqs[i].d_seq, reqs[i].seq_len * sizeof(int32_t), cudaMemcpyDeviceToHost);
+            if (i == 0)
+                first = cur;
+            else
+                same = cur == first && (reqs[i].prm.settle % (uint32_t)(cur.size() - 1)) ==
+                                           (reqs[0].prm.settle % (uint32_t)(first.size() - 1));
+        }
+        if (e == cudaSuccess && same && !first.empty()) {
+            std::string why;
+            cudaKernel_t k = nullptr;
+            if (jit_batch_kernel(first.data(), (uint32_t)first.size() - 1, reqs[0].prm.settle, b->mode, &k, &why))
+                b->jit_kernel = k;
+        }
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(s);
+            destroy(b);
+            return cuda_error(e, "lyap_batch_create: reading the sequences");
+        }
     }
     struct Cand {
         uint32_t tw, th, tpc, bps;
@@ -365,6 +288,7 @@ int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOption
     b->info.tiles_per_chunk = b->tiles_per_chunk;
     b->info.blocks_per_sm = b->blocks_per_sm;
     b->info.threads_per_block = b->threads;
+    b->info.specialised = b->jit_kernel ? 1u : 0u;
     *out = b;
     return LYAP_OK;
 }

@@ -88,8 +88,10 @@ struct Nvrtc {
 };
 
 // One compiled specialisation: the render and volume kernels of both lambda
-// forms, or (a proposal entry, compiled on the first render with a learned
-// proposal) the render kernels with the proposal, render_persistent<Lam, true>.
+// forms (kind KIND_RENDER); the render kernels with the learned proposal,
+// render_persistent<Lam, true> (KIND_PROPOSAL, compiled on the first render
+// with a proposal); or the batch kernels, render_batch<Lam> (KIND_BATCH,
+// compiled for a batch whose requests share one sequence).
 struct Entry {
     bool ok = false;
     std::string error;
@@ -177,13 +179,20 @@ std::string lam_type(const Spec &s, int mode)
            hex64(s.a1) + ">>";
 }
 
-void compile_entry(Entry &e, const Spec &s, bool prop)
+constexpr int KIND_RENDER = 0, KIND_PROPOSAL = 1, KIND_BATCH = 2;
+
+void compile_entry(Entry &e, const Spec &s, int kind)
 {
     Nvrtc &N = g_nvrtc;
     std::vector<std::string> names;
+    const bool prop = kind != KIND_RENDER;   // one kernel per lambda form
     for (int mode = 0; mode < 2; mode++) {
-        if (prop) {
+        if (kind == KIND_PROPOSAL) {
             names.push_back("&lyapgb::render_persistent<" + lam_type(s, mode) + ", true>");
+            continue;
+        }
+        if (kind == KIND_BATCH) {
+            names.push_back("&lyapgb::render_batch<" + lam_type(s, mode) + ">");
             continue;
         }
         names.push_back("&lyapgb::render_persistent<" + lam_type(s, mode) + ">");
@@ -254,7 +263,7 @@ void compile_entry(Entry &e, const Spec &s, bool prop)
 
 // The cached specialisation for this sequence, compiling it on first use.
 // Returns null (with *why set) when the path is unavailable.
-Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string *why, bool prop = false)
+Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string *why, int kind = KIND_RENDER)
 {
     if (jit_disabled_by_env()) {
         *why = "disabled by LYAP_JIT=0";
@@ -274,7 +283,7 @@ Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string 
         return nullptr;
     }
     const Spec s = make_spec(h_seq, L, settle);
-    const std::string key = lam_type(s, 9) + (prop ? "|proposal" : "");
+    const std::string key = lam_type(s, 9) + (kind == KIND_PROPOSAL ? "|proposal" : kind == KIND_BATCH ? "|batch" : "");
     std::lock_guard<std::mutex> lock(g_mu);
     if (g_nvrtc_state == 0) g_nvrtc_state = g_nvrtc.load() ? 1 : -1;
     if (g_nvrtc_state < 0) {
@@ -284,7 +293,7 @@ Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string 
     auto it = g_cache.find(key);
     if (it == g_cache.end()) {
         std::unique_ptr<Entry> e(new Entry());
-        compile_entry(*e, s, prop);
+        compile_entry(*e, s, kind);
         g_compiles++;
         it = g_cache.emplace(key, std::move(e)).first;
     }
@@ -303,7 +312,7 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
 {
     const bool prop = job.prop.bits != nullptr;
     const uint32_t smem = proposal_smem_bytes(job);
-    Entry *e = get_entry(h_seq, job.seq_period, job.prm.settle, why, prop);
+    Entry *e = get_entry(h_seq, job.seq_period, job.prm.settle, why, prop ? KIND_PROPOSAL : KIND_RENDER);
     if (!e) return 0;
     const int sms = device_sm_count();
     if (sms <= 0) {
@@ -335,6 +344,15 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
         std::lock_guard<std::mutex> lock(g_mu);
         g_launches++;
     }
+    return 1;
+}
+
+int jit_batch_kernel(const int32_t *h_seq, uint32_t L, uint32_t settle, uint32_t mode, cudaKernel_t *kernel,
+                     std::string *why)
+{
+    Entry *e = get_entry(h_seq, L, settle, why, KIND_BATCH);
+    if (!e) return 0;
+    *kernel = e->render[mode & 1u];
     return 1;
 }
 

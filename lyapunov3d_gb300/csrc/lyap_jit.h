@@ -38,5 +38,10 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
 int jit_launch_volume(const VolumeJob &job, uint32_t mode, const int32_t *h_seq, unsigned long long *d_stats,
                       uint32_t blocks_per_sm, uint32_t threads, cudaStream_t stream, cudaError_t *launch_err,
                       std::string *why);
+// The batch kernel render_batch<ConstLambda<...>> for one sequence (period L,
+// settle count `settle`) and lambda form: 1 with *kernel set, 0 with the
+// reason in *why.
+int jit_batch_kernel(const int32_t *h_seq, uint32_t L, uint32_t settle, uint32_t mode, cudaKernel_t *kernel,
+                     std::string *why);
 
 }  // namespace lyapgb

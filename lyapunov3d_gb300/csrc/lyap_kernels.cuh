@@ -827,6 +827,138 @@ __global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_bl
     if (stats && lane == 0) atomicMax(stats + LYAP_STAT_T_END, global_ns());
 }
 
+// ----------------------------------------------------------------- batch
+struct BatchTables {
+    const RenderJob *jobs;
+    const uint32_t *chunk_job;    // per chunk: request index
+    const uint32_t *chunk_tile;   // per chunk: first tile within the request
+    uint32_t n_chunks;
+    uint32_t tile_w, tile_h, tiles_per_chunk;
+};
+
+// Many requests in one launch (lyap_batch.cu): persistent warps take chunks
+// of tiles from a global counter; a warp renders one request at a time (its
+// lambda loop must be uniform), so it continues with the next chunk while
+// that belongs to the same request and otherwise lets its rays run out --
+// idle lanes speculate for the rays still running -- before switching.  Lam
+// is RuntimeLambda (any sequences; the library's kernel) or, when every
+// request of the batch has the same sequence, ConstLambda compiled for it at
+// run time, which runs paired rounds as the single-frame render does.
+template <class Lam>
+__global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_blocks)
+    render_batch(const __grid_constant__ BatchTables tb, uint32_t *__restrict__ chunk_counter,
+                 unsigned long long *__restrict__ stats)
+{
+    if (tb.n_chunks == 0) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t tile_px = tb.tile_w * tb.tile_h;
+    const uint32_t slots_per_chunk = tb.tiles_per_chunk * tile_px;
+    LaneStats st = {};
+
+    // the warp's request (uniform)
+    uint32_t cur = tb.chunk_job[0];
+    const RenderJob *J = tb.jobs + cur;
+    Lam lam(J->seq, J->seq_period, J->prm);
+    LyapParams prm = J->prm;
+    CamRays cr = cam_rays(J->cam);
+    uint32_t W = J->width, H = J->height, tiles_x = (W + tb.tile_w - 1) / tb.tile_w;
+    uint32_t n_tiles = tiles_x * ((H + tb.tile_h - 1) / tb.tile_h);
+    bool spec_ok = (prm.jitter == 0.0f) && (prm.nearMultiplier == 1.0f) && !(J->flags & LYAP_FLAG_NO_SPECULATION);
+    bool have_job = false;
+    uint32_t tile0 = 0, slot_next = 0, slot_end = 0;
+    uint32_t pending = 0xffffffffu;   // a claimed chunk of another request
+    bool no_more = false;
+
+    Ray r;
+    r.phase = PH_MARCH0;
+    uint32_t pix = 0;
+    bool active = false;
+
+    for (;;) {
+        // refill idle lanes from the current chunk, claiming chunks of the same request
+        for (;;) {
+            const bool need = !active && have_job;
+            const uint32_t mask = __ballot_sync(FULL, need);
+            if (mask == 0) break;
+            if (slot_next >= slot_end) {
+                if (no_more || pending != 0xffffffffu) break;
+                uint32_t c = 0;
+                if (lane == 0) c = atomicAdd(chunk_counter, 1u);
+                c = __shfl_sync(FULL, c, 0);
+                if (c >= tb.n_chunks) {
+                    no_more = true;
+                    break;
+                }
+                if (tb.chunk_job[c] != cur) {
+                    pending = c;   // switch once this request's rays have run out
+                    break;
+                }
+                tile0 = tb.chunk_tile[c];
+                slot_next = 0;
+                slot_end = slots_per_chunk;
+            }
+            const uint32_t s = slot_next + __popc(mask & ((1u << lane) - 1u));
+            slot_next += __popc(mask);
+            if (need && s < slot_end) {
+                const uint32_t tile = tile0 + s / tile_px, within = s % tile_px;
+                const uint32_t x = (tile % tiles_x) * tb.tile_w + within % tb.tile_w;
+                const uint32_t y = (tile / tiles_x) * tb.tile_h + within / tb.tile_w;
+                if (tile < n_tiles && x < W && y < H) {
+                    pix = x + y * W;
+                    if (ray_init(r, cr, prm, x, y)) {
+                        active = true;
+                    } else {
+                        r.nm = r.nh = r.ns = 0;
+                        finish_pixel(J->rgba, J->points, J->counts, pix, r, false, cr.C, J->lights, J->n_lights,
+                                     J->light_model, st);
+                    }
+                }
+            }
+        }
+        const uint32_t amask = __ballot_sync(FULL, active);
+        if (amask == 0) {
+            // every ray of this warp has ended: move to the pending request, or claim one
+            uint32_t c = pending;
+            if (c == 0xffffffffu) {
+                if (no_more) break;
+                if (lane == 0) c = atomicAdd(chunk_counter, 1u);
+                c = __shfl_sync(FULL, c, 0);
+                if (c >= tb.n_chunks) break;
+            }
+            pending = 0xffffffffu;
+            cur = tb.chunk_job[c];
+            J = tb.jobs + cur;
+            lam = Lam(J->seq, J->seq_period, J->prm);
+            prm = J->prm;
+            cr = cam_rays(J->cam);
+            W = J->width;
+            H = J->height;
+            tiles_x = (W + tb.tile_w - 1) / tb.tile_w;
+            n_tiles = tiles_x * ((H + tb.tile_h - 1) / tb.tile_h);
+            spec_ok = (prm.jitter == 0.0f) && (prm.nearMultiplier == 1.0f) && !(J->flags & LYAP_FLAG_NO_SPECULATION);
+            have_job = true;
+            tile0 = tb.chunk_tile[c];
+            slot_next = 0;
+            slot_end = slots_per_chunk;
+            continue;
+        }
+        int res;
+        if constexpr (RenderTuning<Lam>::pairs) {
+            const bool fixed_step = (prm.jitter == 0.0f) && (prm.nearMultiplier == 1.0f);
+            res = sample_round_pair<false>(r, active, amask, lam, prm, fixed_step, spec_ok, false, PropGrid{}, st);
+        } else {
+            res = sample_round<false>(r, active, amask, lam, prm, spec_ok, false, PropGrid{}, st);
+        }
+        if (active && res != RAY_CONTINUE) {
+            finish_pixel(J->rgba, J->points, J->counts, pix, r, res == RAY_HIT, cr.C, J->lights, J->n_lights,
+                         J->light_model, st);
+            active = false;
+        }
+    }
+    flush_stats(stats, st, FULL);
+}
+
+
 // ----------------------------------------------------------------- volume
 __device__ __forceinline__ float voxel_coord(float lo, float hi, uint32_t i, uint32_t n)
 {

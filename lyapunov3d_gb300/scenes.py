@@ -201,14 +201,15 @@ def full_volume(n=512, seed=1):
                           (4.0, 4.0, 4.0), seq, prm)
 
 
-def batch_workloads(seed=4, scale=1, n_render=256, n_slices=32):
+def batch_workloads(seed=4, scale=1, n_render=256, n_slices=32, one_seq=None):
     """The batched workload: n_render frames with resolution drawn from
     {256^2, 512^2, 1024^2, 1920x1080} (each side divided by `scale`), 128-1024
     steps per ray, 200 settle + 200-4000 accumulated iterations (log-uniform),
     sequences of length 2-16 over {A, B, C}; plus n_slices 4-D slices: the
     same kind of frame with sequences over {A, B, C, D} and D uniform in
     [2.5, 4].  Cameras orbit the [2, 4]^3 box at distance 5-8; thresholds are
-    the reference's defaults."""
+    the reference's defaults.  one_seq: every request takes this sequence
+    instead (the frames of one field; everything else is drawn as above)."""
     rng = SplitMix64(0x4C594150_BA7C0000 | seed)
     sizes = [(256, 256), (512, 512), (1024, 1024), (1920, 1080)]
     out = []
@@ -222,6 +223,8 @@ def batch_workloads(seed=4, scale=1, n_render=256, n_slices=32):
         seq = random_sequence(rng, L, "ABCD" if slice4d else "ABC")
         if slice4d and "D" not in seq:
             seq = seq[:-1] + "D"
+        if one_seq is not None:
+            seq = one_seq
         d = rng.uniform(2.5, 4.0) if slice4d else 2.1
         q = uniform_quaternion(rng)
         dist = rng.uniform(5.0, 8.0)

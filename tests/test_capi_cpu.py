@@ -199,8 +199,8 @@ def test_abi_struct_sizes_match_c(tmp_path):
         "LyapNetTrainOptions": (capi.LyapNetTrainOptions, ["steps", "lr", "seed", "box_lo", "box_hi", "h_loss"]),
         "LyapVolumeExt": (capi.LyapVolumeExt, ["variant", "d_stats", "flags", "h_seq"]),
         "LyapRequest": (capi.LyapRequest, ["prm", "d_seq", "d_counts", "seq_len", "flags"]),
-        "LyapBatchOptions": (capi.LyapBatchOptions, ["autotune", "d_stats"]),
-        "LyapBatchInfo": (capi.LyapBatchInfo, ["candidates", "tuned_ms"]),
+        "LyapBatchOptions": (capi.LyapBatchOptions, ["autotune", "flags", "d_stats"]),
+        "LyapBatchInfo": (capi.LyapBatchInfo, ["candidates", "specialised", "tuned_ms"]),
     }
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "lyap_gb300.h"', "int main(void) {"]
     for name, (_, fields) in checks.items():

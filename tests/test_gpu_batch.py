@@ -83,3 +83,40 @@ def test_batch_rejects_bad_request():
     with pytest.raises(capi.LyapError) as e:
         capi.Batch([q])
     assert e.value.code == capi.LYAP_ERR_INVALID_ARG and "request 0" in e.value.message
+
+
+def _one_sequence_batch(seq):
+    wls = scenes.batch_workloads(seed=9, scale=32, n_render=10, n_slices=0, one_seq=seq)
+    for wl in wls:   # keep the iteration counts test-sized
+        wl.params.settle = 20 + 7 * (wl.params.accum % 3)   # settle counts differing by whole periods
+        wl.params.accum = max(20, wl.params.accum // 40)
+        wl.params.depth = max(32.0, wl.params.depth / 8)
+    return wls
+
+
+@pytest.mark.parametrize("variant", [capi.VARIANT_PLAIN, capi.VARIANT_PRODUCT])
+def test_one_sequence_batch_runs_the_specialised_kernel(variant):
+    """A batch whose requests share one sequence (and settle count mod its
+    period) runs the batch kernel compiled for that sequence at run time
+    (paired rounds for the product form); every request still gets exactly
+    lyap_render's bytes.  LYAP_FLAG_NO_JIT keeps the library's kernel."""
+    dev = torch.device("cuda:0")
+    wls = _one_sequence_batch("ABCCABB")   # period 7: settle 20, 27, 34 share settle mod 7
+    db = DeviceBatch(wls, device=dev, variant=variant, autotune=False, counts=True)
+    db.run()
+    torch.cuda.synchronize()
+    info = db.batch.info()
+    if not capi.jit_info()[0]:
+        pytest.skip("NVRTC unavailable")
+    assert info.specialised == 1
+    for wl, bf in zip(wls, db.frames):
+        f = DeviceFrame(wl, device=dev, counts=True)
+        f.run(variant)
+        torch.cuda.synchronize()
+        assert torch.equal(bf.d_rgba, f.d_rgba), wl.name
+        assert torch.equal(bf.d_points.view(torch.int32), f.d_points.view(torch.int32)), wl.name
+        assert torch.equal(bf.d_counts, f.d_counts), wl.name
+    off = DeviceBatch(wls, device=dev, variant=variant, autotune=False, counts=True, flags=capi.FLAG_NO_JIT)
+    assert off.batch.info().specialised == 0
+    mixed = DeviceBatch(_small_batch(), device=dev, variant=variant, autotune=False)
+    assert mixed.batch.info().specialised == 0
