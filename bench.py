@@ -72,6 +72,8 @@ def parse_args():
     ap.add_argument("--batch-scale", type=int, default=1, help="--report batch: divide every image side by this")
     ap.add_argument("--batch-seq", default=None,
                     help="--report batch: every request takes this sequence (the frames of one field)")
+    ap.add_argument("--batch-jit-groups", type=int, default=0,
+                    help="--report batch: sequence groups compiled for (0: the library's default; -1: none)")
     return ap.parse_args()
 
 
@@ -689,8 +691,9 @@ def run_batch_report(args):
     from lyapunov3d_gb300.device import DeviceBatch
     dev = torch.device("cuda", 0)
     wls = scenes.batch_workloads(seed=4, scale=args.batch_scale, one_seq=args.batch_seq)
+    jit = {"flags": capi.FLAG_NO_JIT} if args.batch_jit_groups < 0 else {"jit_groups": args.batch_jit_groups}
     t0 = time.perf_counter()
-    db = DeviceBatch(wls, device=dev, variant=capi.VARIANT_PRODUCT, autotune=True, counts=True)
+    db = DeviceBatch(wls, device=dev, variant=capi.VARIANT_PRODUCT, autotune=True, counts=True, **jit)
     t_create = time.perf_counter() - t0
     stream = torch.cuda.current_stream(dev)
     db.run(stream)
@@ -712,7 +715,9 @@ def run_batch_report(args):
     st = db.stats()
     print(json.dumps({
         "report": "batch", "requests": len(wls), "pixels": sum(w.width * w.height for w in wls),
-        "scale": args.batch_scale, "one_sequence": args.batch_seq, "specialised": int(info.specialised),
+        "scale": args.batch_scale, "one_sequence": args.batch_seq,
+        "sequence_groups": len({(w.seq, w.params.settle % len(w.seq)) for w in wls}),
+        "jit_groups": args.batch_jit_groups, "specialised_requests": int(info.specialised),
         "create_s": t_create, "ms_per_launch": ms, "launch_ms": times,
         "plain_iters_per_launch": iters, "g_iters_per_s": iters / (ms * 1e-3) / 1e9,
         "tuned": {"tile": [info.tile_w, info.tile_h], "tiles_per_chunk": info.tiles_per_chunk,

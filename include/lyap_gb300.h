@@ -453,17 +453,32 @@ typedef struct {
     uint32_t variant;             /* LYAP_VARIANT_* for every request */
     uint32_t autotune;            /* 1: time the candidate launch shapes */
     uint32_t tile_w, tile_h, tiles_per_chunk, blocks_per_sm;   /* used when autotune = 0 */
-    uint32_t flags;               /* LYAP_FLAG_NO_JIT: never the kernel compiled for a
-                                     batch whose requests share one sequence */
+    uint32_t flags;               /* LYAP_FLAG_NO_JIT: every request on the library's
+                                     kernel, none compiled for its sequence */
     unsigned long long *d_stats;  /* optional device LYAP_STAT_COUNT array */
+    uint32_t jit_groups;          /* at most this many sequence groups get a kernel
+                                     compiled for them (0: LYAP_BATCH_JIT_GROUPS_DEFAULT;
+                                     at most LYAP_BATCH_JIT_GROUPS_MAX).  A caller built
+                                     without this field passes size =
+                                     offsetof(LyapBatchOptions, jit_groups). */
 } LyapBatchOptions;
+
+/* Requests with the same sequence (and settle count mod its period) form a
+ * group; the batch kernel is compiled at run time (NVRTC, parallel host
+ * threads, cached for the process) for the heaviest groups that carry at
+ * least 1/200 of the batch's estimated cost, and each such group runs as a
+ * launch of its own in the batch's graph; the other requests run the
+ * library's kernel.  A batch of one sequence is one specialised launch. */
+#define LYAP_BATCH_JIT_GROUPS_DEFAULT 64u
+#define LYAP_BATCH_JIT_GROUPS_MAX 255u
 
 typedef struct {
     uint32_t size, requests, chunks;
     uint32_t tile_w, tile_h, tiles_per_chunk, blocks_per_sm, threads_per_block;
     uint32_t candidates;
-    uint32_t specialised;         /* 1: every request has the same sequence, and the
-                                     batch runs the kernel compiled for it at run time */
+    uint32_t specialised;         /* requests run by kernels compiled for their
+                                     sequence at run time (all of them for a batch of
+                                     one sequence; 0 with LYAP_FLAG_NO_JIT) */
     float tuned_ms[16];           /* time of each candidate on the sample */
 } LyapBatchInfo;
 

@@ -46,6 +46,8 @@ MAX_LIGHTS = 16
  STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END, STAT_PROPOSAL_REWOUND, STAT_TAIL_HANDOVERS) = range(21)
 STAT_COUNT = 21
 PROPOSAL_GRID_DEFAULT = 64
+BATCH_JIT_GROUPS_DEFAULT = 64
+BATCH_JIT_GROUPS_MAX = 255
 # the proposal margin the library's users are pointed to: the smallest of the
 # measured margins at which the 1080p bench frame keeps >= 99.9 % of its
 # surface pixels (bench.py --report proposal)
@@ -116,7 +118,7 @@ assert ctypes.sizeof(LyapRequest) == 352
 class LyapBatchOptions(ctypes.Structure):
     _fields_ = [("size", c_uint32), ("variant", c_uint32), ("autotune", c_uint32), ("tile_w", c_uint32),
                 ("tile_h", c_uint32), ("tiles_per_chunk", c_uint32), ("blocks_per_sm", c_uint32),
-                ("flags", c_uint32), ("d_stats", c_void_p)]
+                ("flags", c_uint32), ("d_stats", c_void_p), ("jit_groups", c_uint32)]
 
     def __init__(self, **kw):
         super().__init__()

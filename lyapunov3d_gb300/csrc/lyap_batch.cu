@@ -1,6 +1,5 @@
-// lyap_batch.cu -- many render requests in one launch (persistent warps over
-// a device work queue), captured in a CUDA graph, launch shape picked by an
-// autotuner.
+// lyap_batch.cu -- many render requests in one graph launch (persistent
+// warps over device work queues), launch shape picked by an autotuner.
 //
 // The reference renders one frame per launch (lyap_interactive.cu:711); a
 // sweep of frames (scale.pl) is a loop of whole program runs.  Here a batch
@@ -12,24 +11,39 @@
 // it continues with the next chunk while that belongs to the same request
 // and otherwise lets its rays run out -- idle lanes speculate for the rays
 // still running (sample_round) -- before switching (render_batch,
-// lyap_kernels.cuh).  When every request has the same sequence (and settle
-// count mod its period) -- the frames of an animation of one field -- the
-// kernel is compiled for that sequence at run time (ConstLambda, paired
-// rounds; LYAP_FLAG_NO_JIT in the options keeps the library's kernel).
+// lyap_kernels.cuh).
+//
+// Sequences.  Requests that share a sequence (and settle count mod its
+// period) form a group.  For the heaviest groups -- up to
+// LyapBatchOptions.jit_groups (default LYAP_BATCH_JIT_GROUPS_DEFAULT), each
+// carrying at least 1/200 of the batch's estimated cost -- the batch kernel
+// is compiled for the group's sequence at run time (ConstLambda, paired
+// rounds), the compiles running in parallel host threads; the other
+// requests run the library's kernel for any sequence (RuntimeLambda).  Each
+// group is a launch of its own, over its own chunk list and counter; the
+// launches are parallel branches of the graph, so the blocks of one take the
+// SMs that another's leave at its end (a request alone in a launch would
+// otherwise pay a frame's end on its own).  A batch of one sequence (the
+// frames of an animation of one field) is a single specialised launch.
+// LYAP_FLAG_NO_JIT keeps every request on the library's kernel.
 //
 // Autotuner: the tile shape (32x1, 8x4, 16x16), the tiles per chunk (1, 4)
 // and the resident blocks per SM (3, 4) are timed on every 8th chunk of the
-// batch itself and the fastest kept; the whole launch (counter reset +
-// kernel) is then captured once in a graph that lyap_batch_run replays.
+// batch itself (all launches) and the fastest kept; the launches (counter
+// resets + kernels) are then captured once in a graph that lyap_batch_run
+// replays.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
-#include <vector>
-
 #include <string>
+#include <thread>
+#include <utility>
+#include <vector>
 
 #include "lyap_internal.h"
 #include "lyap_jit.h"
@@ -41,19 +55,29 @@ namespace lyapgb {
 
 using namespace lyapgb;
 
+// One launch of the batch: a kernel and the requests it renders.
+struct BatchPart {
+    cudaKernel_t kernel = nullptr;   // compiled for the part's sequence; null: the library's kernel
+    std::vector<uint32_t> jobs;      // request indices
+    uint32_t *d_chunks = nullptr;    // chunk_job then chunk_tile
+    uint32_t n_chunks = 0;
+};
+
 struct LyapBatch {
     int device = 0;
     uint32_t n_jobs = 0, mode = 0;
     RenderJob *d_jobs = nullptr;
-    uint32_t *d_counter = nullptr;
+    uint32_t *d_counter = nullptr;   // one chunk counter per part
     unsigned long long *d_stats = nullptr;
     std::vector<RenderJob> jobs;
     std::vector<double> cost;
-    // chosen launch shape and its chunk list
+    std::vector<BatchPart> parts;
+    // the parts run concurrently: one stream each, forked from and joined
+    // to the launching stream by events (parallel branches of the graph)
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;   // [0]: the fork; [1 + i]: part i done
+    // chosen launch shape
     uint32_t tile_w = 16, tile_h = 16, tiles_per_chunk = 1, blocks_per_sm = 3, threads = 128;
-    uint32_t *d_chunks = nullptr;   // chunk_job then chunk_tile
-    uint32_t n_chunks = 0;
-    cudaKernel_t jit_kernel = nullptr;   // the kernel compiled for the batch's one sequence, if any
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     LyapBatchInfo info;
@@ -61,11 +85,13 @@ struct LyapBatch {
 
 namespace {
 
-void build_chunks(const LyapBatch &b, uint32_t tw, uint32_t th, uint32_t tpc, uint32_t sample_every,
-                  std::vector<uint32_t> &cj, std::vector<uint32_t> &ct)
+// counters: one 32-bit word per part
+constexpr uint32_t kMaxParts = LYAP_BATCH_JIT_GROUPS_MAX + 1;
+
+void build_chunks(const LyapBatch &b, const std::vector<uint32_t> &jobs, uint32_t tw, uint32_t th, uint32_t tpc,
+                  uint32_t sample_every, std::vector<uint32_t> &cj, std::vector<uint32_t> &ct)
 {
-    std::vector<uint32_t> order(b.n_jobs);
-    for (uint32_t i = 0; i < b.n_jobs; i++) order[i] = i;
+    std::vector<uint32_t> order(jobs);
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c) { return b.cost[a] > b.cost[c]; });
     cj.clear();
     ct.clear();
@@ -81,46 +107,168 @@ void build_chunks(const LyapBatch &b, uint32_t tw, uint32_t th, uint32_t tpc, ui
     }
 }
 
-cudaError_t upload_chunks(LyapBatch &b, const std::vector<uint32_t> &cj, const std::vector<uint32_t> &ct,
+// every part's chunk list for one launch shape (sample_every > 1: a sample of it)
+cudaError_t upload_chunks(LyapBatch &b, uint32_t tw, uint32_t th, uint32_t tpc, uint32_t sample_every,
                           cudaStream_t s)
 {
-    if (b.d_chunks) cudaFreeAsync(b.d_chunks, s);
-    b.d_chunks = nullptr;
-    b.n_chunks = (uint32_t)cj.size();
-    cudaError_t e = cudaMallocAsync((void **)&b.d_chunks, sizeof(uint32_t) * 2 * (cj.size() + 1), s);
-    if (e != cudaSuccess) return e;
-    e = cudaMemcpyAsync(b.d_chunks, cj.data(), sizeof(uint32_t) * cj.size(), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(b.d_chunks + cj.size(), ct.data(), sizeof(uint32_t) * ct.size(), cudaMemcpyHostToDevice, s);
+    std::vector<uint32_t> cj, ct;
+    for (BatchPart &p : b.parts) {
+        build_chunks(b, p.jobs, tw, th, tpc, sample_every, cj, ct);
+        if (p.d_chunks) cudaFreeAsync(p.d_chunks, s);
+        p.d_chunks = nullptr;
+        p.n_chunks = (uint32_t)cj.size();
+        cudaError_t e = cudaMallocAsync((void **)&p.d_chunks, sizeof(uint32_t) * 2 * (cj.size() + 1), s);
+        if (e == cudaSuccess && !cj.empty())
+            e = cudaMemcpyAsync(p.d_chunks, cj.data(), sizeof(uint32_t) * cj.size(), cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && !ct.empty())
+            e = cudaMemcpyAsync(p.d_chunks + cj.size(), ct.data(), sizeof(uint32_t) * ct.size(),
+                                cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Streams and events for running the parts concurrently.
+cudaError_t make_streams(LyapBatch &b)
+{
+    if (b.parts.size() < 2) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    for (size_t i = 0; i < b.parts.size() && e == cudaSuccess; i++) {
+        cudaStream_t st = nullptr;
+        e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) b.streams.push_back(st);
+    }
+    for (size_t i = 0; i <= b.parts.size() && e == cudaSuccess; i++) {
+        cudaEvent_t ev = nullptr;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) b.events.push_back(ev);
+    }
     return e;
 }
 
-cudaError_t launch_batch(const LyapBatch &b, uint32_t tw, uint32_t th, uint32_t tpc, uint32_t bps, const uint32_t *chunks,
-                         uint32_t n_chunks, unsigned long long *stats, cudaStream_t s)
+// The batch's launches, one per part (reset the part's counter, run its
+// kernel), all at once: forked from `s` onto the parts' streams and joined
+// back, so that one part's blocks take the SMs another part's leave at its
+// end.  The parts come heaviest first, the library's kernel last.
+cudaError_t launch_batch(const LyapBatch &b, uint32_t tw, uint32_t th, uint32_t tpc, uint32_t bps,
+                         unsigned long long *stats, cudaStream_t s)
 {
-    BatchTables tb;
-    tb.jobs = b.d_jobs;
-    tb.chunk_job = chunks;
-    tb.chunk_tile = chunks + n_chunks;
-    tb.n_chunks = n_chunks;
-    tb.tile_w = tw;
-    tb.tile_h = th;
-    tb.tiles_per_chunk = tpc;
     const int sms = device_sm_count();
     if (sms <= 0) return cudaErrorNoDevice;
-    cudaError_t e = cudaMemsetAsync(b.d_counter, 0, sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
+    const bool fork = b.streams.size() == b.parts.size() && b.parts.size() > 1;
+    const uint32_t tpb = b.threads;
     const uint32_t grid = (uint32_t)sms * bps;
-    if (b.jit_kernel) {
-        uint32_t *counter = b.d_counter;
-        void *args[] = {&tb, &counter, &stats};
-        return cudaLaunchKernel((const void *)b.jit_kernel, dim3(grid), dim3(b.threads), args, 0, s);
+    if (fork) {
+        cudaError_t e = cudaEventRecord(b.events[0], s);
+        if (e != cudaSuccess) return e;
     }
-    if (b.mode == MODE_PRODUCT)
-        render_batch<RuntimeLambda<MODE_PRODUCT>><<<grid, b.threads, 0, s>>>(tb, b.d_counter, stats);
-    else
-        render_batch<RuntimeLambda<MODE_PLAIN>><<<grid, b.threads, 0, s>>>(tb, b.d_counter, stats);
-    return cudaGetLastError();
+    for (size_t i = 0; i < b.parts.size(); i++) {
+        const BatchPart &p = b.parts[i];
+        if (p.n_chunks == 0) continue;
+        cudaStream_t ps = s;
+        if (fork) {
+            ps = b.streams[i];
+            cudaError_t e = cudaStreamWaitEvent(ps, b.events[0], 0);
+            if (e != cudaSuccess) return e;
+        }
+        BatchTables tb;
+        tb.jobs = b.d_jobs;
+        tb.chunk_job = p.d_chunks;
+        tb.chunk_tile = p.d_chunks + p.n_chunks;
+        tb.n_chunks = p.n_chunks;
+        tb.tile_w = tw;
+        tb.tile_h = th;
+        tb.tiles_per_chunk = tpc;
+        uint32_t *counter = b.d_counter + i;
+        cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), ps);
+        if (e != cudaSuccess) return e;
+        if (p.kernel) {
+            void *args[] = {&tb, &counter, &stats};
+            e = cudaLaunchKernel((const void *)p.kernel, dim3(grid), dim3(tpb), args, 0, ps);
+        } else {
+            if (b.mode == MODE_PRODUCT)
+                render_batch<RuntimeLambda<MODE_PRODUCT>><<<grid, tpb, 0, ps>>>(tb, counter, stats);
+            else
+                render_batch<RuntimeLambda<MODE_PLAIN>><<<grid, tpb, 0, ps>>>(tb, counter, stats);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess && fork) e = cudaEventRecord(b.events[1 + i], ps);
+        if (e == cudaSuccess && fork) e = cudaStreamWaitEvent(s, b.events[1 + i], 0);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Group the requests by sequence (symbols and settle count mod the period)
+// and compile the batch kernel for the heaviest groups, in parallel host
+// threads; fills b.parts (the specialised groups first, then one part for
+// everything else).  Reads every request's sequence back from the device.
+cudaError_t plan_parts(LyapBatch &b, const LyapRequest *reqs, uint32_t max_groups)
+{
+    using Key = std::pair<std::vector<int32_t>, uint32_t>;
+    std::map<Key, std::vector<uint32_t>> groups;
+    std::vector<int32_t> seq;
+    for (uint32_t i = 0; i < b.n_jobs; i++) {
+        seq.resize(reqs[i].seq_len);
+        cudaError_t e = cudaMemcpy(seq.data(), reqs[i].d_seq, reqs[i].seq_len * sizeof(int32_t),
+                                   cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return e;
+        const uint32_t L = reqs[i].seq_len - 1;
+        groups[Key(seq, reqs[i].prm.settle % L)].push_back(i);
+    }
+    double total = 0;
+    for (double c : b.cost) total += c;
+    struct Group {
+        const Key *key;
+        const std::vector<uint32_t> *jobs;
+        double cost;
+        uint32_t settle;
+        cudaKernel_t kernel;
+    };
+    std::vector<Group> cand;
+    for (auto &g : groups) {
+        double c = 0;
+        for (uint32_t j : g.second) c += b.cost[j];
+        const uint32_t L = (uint32_t)g.first.first.size() - 1;
+        if (L <= LYAP_JIT_MAX_PERIOD && (groups.size() == 1 || c * 200.0 >= total))
+            cand.push_back(Group{&g.first, &g.second, c, reqs[g.second[0]].prm.settle, nullptr});
+    }
+    std::stable_sort(cand.begin(), cand.end(), [](const Group &a, const Group &c) { return a.cost > c.cost; });
+    if (cand.size() > max_groups) cand.resize(max_groups);
+    // compile in parallel; a group whose compile fails stays on the library's kernel
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nthreads = std::min<size_t>(cand.size(), std::min(hw, 16u));
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+        cudaSetDevice(b.device);
+        for (size_t i; (i = next.fetch_add(1)) < cand.size();) {
+            std::string why;
+            cudaKernel_t k = nullptr;
+            const std::vector<int32_t> &sq = cand[i].key->first;
+            if (jit_batch_kernel(sq.data(), (uint32_t)sq.size() - 1, cand[i].settle, b.mode, &k, &why))
+                cand[i].kernel = k;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (size_t t = 1; t < nthreads; t++) pool.emplace_back(work);
+    if (nthreads) work();
+    for (auto &t : pool) t.join();
+    std::vector<char> special(b.n_jobs, 0);
+    b.parts.clear();
+    for (const Group &g : cand) {
+        if (!g.kernel) continue;
+        BatchPart p;
+        p.kernel = g.kernel;
+        p.jobs = *g.jobs;
+        for (uint32_t j : p.jobs) special[j] = 1;
+        b.info.specialised += (uint32_t)p.jobs.size();
+        b.parts.push_back(std::move(p));
+    }
+    BatchPart rest;
+    for (uint32_t j = 0; j < b.n_jobs; j++)
+        if (!special[j]) rest.jobs.push_back(j);
+    if (!rest.jobs.empty()) b.parts.push_back(std::move(rest));
+    return cudaSuccess;
 }
 
 void destroy(LyapBatch *b)
@@ -128,7 +276,10 @@ void destroy(LyapBatch *b)
     if (!b) return;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->d_chunks) cudaFree(b->d_chunks);
+    for (BatchPart &p : b->parts)
+        if (p.d_chunks) cudaFree(p.d_chunks);
+    for (cudaEvent_t ev : b->events) cudaEventDestroy(ev);
+    for (cudaStream_t st : b->streams) cudaStreamDestroy(st);
     if (b->d_jobs) cudaFree(b->d_jobs);
     if (b->d_counter) cudaFree(b->d_counter);
     delete b;
@@ -141,9 +292,14 @@ extern "C" {
 int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOptions *opt, LyapBatch **out)
 {
     if (!reqs || !out || n == 0) return set_error(LYAP_ERR_INVALID_ARG, "lyap_batch_create: no requests");
-    if (opt && opt->size != sizeof(LyapBatchOptions))
-        return set_error(LYAP_ERR_INVALID_ARG, "lyap_batch_create: LyapBatchOptions.size is %u, expected %zu",
-                         opt->size, sizeof(LyapBatchOptions));
+    if (opt && opt->size != sizeof(LyapBatchOptions) && opt->size != offsetof(LyapBatchOptions, jit_groups))
+        return set_error(LYAP_ERR_INVALID_ARG, "lyap_batch_create: LyapBatchOptions.size is %u, expected %zu (or %zu)",
+                         opt->size, sizeof(LyapBatchOptions), offsetof(LyapBatchOptions, jit_groups));
+    // the field exists only in the full-size struct
+    const uint32_t jit_groups_opt = (opt && opt->size == sizeof(LyapBatchOptions)) ? opt->jit_groups : 0u;
+    if (jit_groups_opt > LYAP_BATCH_JIT_GROUPS_MAX)
+        return set_error(LYAP_ERR_INVALID_ARG, "lyap_batch_create: jit_groups %u > %u", jit_groups_opt,
+                         (unsigned)LYAP_BATCH_JIT_GROUPS_MAX);
     if (opt && opt->variant > LYAP_VARIANT_PRODUCT)
         return set_error(LYAP_ERR_INVALID_ARG, "lyap_batch_create: unknown variant %u", opt->variant);
     *out = nullptr;
@@ -180,38 +336,32 @@ int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOption
     cudaStream_t s = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_jobs, sizeof(RenderJob) * n);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_counter, 256);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_counter, sizeof(uint32_t) * kMaxParts);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_jobs, b->jobs.data(), sizeof(RenderJob) * n, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) {
         if (s) cudaStreamDestroy(s);
         destroy(b);
         return cuda_error(e, "lyap_batch_create: device tables");
     }
-    // one sequence for every request (same symbols, same settle count mod its
-    // period): the batch kernel compiled for it
-    if (!(opt && (opt->flags & LYAP_FLAG_NO_JIT))) {
-        std::vector<int32_t> first, cur;
-        bool same = true;
-        for (uint32_t i = 0; i < n && same && e == cudaSuccess; i++) {
-            cur.resize(reqs[i].seq_len);
-            e = cudaMemcpy(cur.data(), reqs[i].d_seq, reqs[i].seq_len * sizeof(int32_t), cudaMemcpyDeviceToHost);
-            if (i == 0)
-                first = cur;
-            else
-                same = cur == first && (reqs[i].prm.settle % (uint32_t)(cur.size() - 1)) ==
-                                           (reqs[0].prm.settle % (uint32_t)(first.size() - 1));
-        }
-        if (e == cudaSuccess && same && !first.empty()) {
-            std::string why;
-            cudaKernel_t k = nullptr;
-            if (jit_batch_kernel(first.data(), (uint32_t)first.size() - 1, reqs[0].prm.settle, b->mode, &k, &why))
-                b->jit_kernel = k;
-        }
+    // the requests grouped by sequence; kernels compiled for the heaviest groups
+    const bool jit = !(opt && (opt->flags & LYAP_FLAG_NO_JIT));
+    if (jit) {
+        e = plan_parts(*b, reqs, jit_groups_opt ? jit_groups_opt : LYAP_BATCH_JIT_GROUPS_DEFAULT);
         if (e != cudaSuccess) {
             cudaStreamDestroy(s);
             destroy(b);
             return cuda_error(e, "lyap_batch_create: reading the sequences");
         }
+    } else {
+        BatchPart all;
+        for (uint32_t j = 0; j < n; j++) all.jobs.push_back(j);
+        b->parts.push_back(std::move(all));
+    }
+    e = make_streams(*b);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        destroy(b);
+        return cuda_error(e, "lyap_batch_create: streams");
     }
     struct Cand {
         uint32_t tw, th, tpc, bps;
@@ -227,7 +377,6 @@ int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOption
         cands.push_back(Cand{opt->tile_w ? opt->tile_w : 16u, opt->tile_h ? opt->tile_h : 16u,
                              opt->tiles_per_chunk ? opt->tiles_per_chunk : 1u, opt->blocks_per_sm ? opt->blocks_per_sm : 3u});
     }
-    std::vector<uint32_t> cj, ct;
     size_t best = 0;
     float best_ms = -1.0f;
     if (cands.size() > 1) {
@@ -237,11 +386,10 @@ int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOption
         cudaEventCreate(&e1);
         for (size_t i = 0; i < cands.size() && e == cudaSuccess; i++) {
             const Cand &c = cands[i];
-            build_chunks(*b, c.tw, c.th, c.tpc, 8, cj, ct);
-            e = upload_chunks(*b, cj, ct, s);
+            e = upload_chunks(*b, c.tw, c.th, c.tpc, 8, s);
             if (e != cudaSuccess) break;
             cudaEventRecord(e0, s);
-            e = launch_batch(*b, c.tw, c.th, c.tpc, c.bps, b->d_chunks, b->n_chunks, nullptr, s);
+            e = launch_batch(*b, c.tw, c.th, c.tpc, c.bps, nullptr, s);
             cudaEventRecord(e1, s);
             if (e == cudaSuccess) e = cudaEventSynchronize(e1);
             float ms = 0;
@@ -262,15 +410,13 @@ int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOption
         b->tile_h = c.th;
         b->tiles_per_chunk = c.tpc;
         b->blocks_per_sm = c.bps;
-        build_chunks(*b, c.tw, c.th, c.tpc, 1, cj, ct);
-        e = upload_chunks(*b, cj, ct, s);
+        e = upload_chunks(*b, c.tw, c.th, c.tpc, 1, s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     // capture the launch (counter reset + kernel) once; lyap_batch_run replays it
     if (e == cudaSuccess) e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        cudaError_t le = launch_batch(*b, b->tile_w, b->tile_h, b->tiles_per_chunk, b->blocks_per_sm, b->d_chunks,
-                                      b->n_chunks, b->d_stats, s);
+        cudaError_t le = launch_batch(*b, b->tile_w, b->tile_h, b->tiles_per_chunk, b->blocks_per_sm, b->d_stats, s);
         e = cudaStreamEndCapture(s, &b->graph);
         if (le != cudaSuccess) e = le;
     }
@@ -282,13 +428,13 @@ int lyap_batch_create(const LyapRequest *reqs, uint32_t n, const LyapBatchOption
     }
     b->info.size = sizeof(LyapBatchInfo);
     b->info.requests = n;
-    b->info.chunks = b->n_chunks;
+    b->info.chunks = 0;
+    for (const BatchPart &p : b->parts) b->info.chunks += p.n_chunks;
     b->info.tile_w = b->tile_w;
     b->info.tile_h = b->tile_h;
     b->info.tiles_per_chunk = b->tiles_per_chunk;
     b->info.blocks_per_sm = b->blocks_per_sm;
     b->info.threads_per_block = b->threads;
-    b->info.specialised = b->jit_kernel ? 1u : 0u;
     *out = b;
     return LYAP_OK;
 }

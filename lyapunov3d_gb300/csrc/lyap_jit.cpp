@@ -90,9 +90,12 @@ struct Nvrtc {
 // One compiled specialisation: the render and volume kernels of both lambda
 // forms (kind KIND_RENDER); the render kernels with the learned proposal,
 // render_persistent<Lam, true> (KIND_PROPOSAL, compiled on the first render
-// with a proposal); or the batch kernels, render_batch<Lam> (KIND_BATCH,
-// compiled for a batch whose requests share one sequence).
+// with a proposal); or the batch kernel of one lambda form, render_batch<Lam>
+// (KIND_BATCH + form, compiled for the requests of a batch that share one
+// sequence; a batch compiles several in parallel threads).
 struct Entry {
+    std::once_flag once;   // the compile, done once outside the cache's lock
+    bool done = false;     // the compile has finished (read and written under g_mu)
     bool ok = false;
     std::string error;
     cudaLibrary_t lib = nullptr;
@@ -179,25 +182,30 @@ std::string lam_type(const Spec &s, int mode)
            hex64(s.a1) + ">>";
 }
 
+// KIND_BATCH + mode: the batch kernel of lambda form `mode` only
 constexpr int KIND_RENDER = 0, KIND_PROPOSAL = 1, KIND_BATCH = 2;
 
 void compile_entry(Entry &e, const Spec &s, int kind)
 {
     Nvrtc &N = g_nvrtc;
+    // each kernel's name expression and where its handle goes
     std::vector<std::string> names;
-    const bool prop = kind != KIND_RENDER;   // one kernel per lambda form
+    std::vector<cudaKernel_t *> slots;
     for (int mode = 0; mode < 2; mode++) {
         if (kind == KIND_PROPOSAL) {
             names.push_back("&lyapgb::render_persistent<" + lam_type(s, mode) + ", true>");
-            continue;
-        }
-        if (kind == KIND_BATCH) {
+            slots.push_back(&e.render[mode]);
+        } else if (kind >= KIND_BATCH) {
+            if (mode != kind - KIND_BATCH) continue;
             names.push_back("&lyapgb::render_batch<" + lam_type(s, mode) + ">");
-            continue;
+            slots.push_back(&e.render[mode]);
+        } else {
+            names.push_back("&lyapgb::render_persistent<" + lam_type(s, mode) + ">");
+            slots.push_back(&e.render[mode]);
+            names.push_back("&lyapgb::volume_sweep<" + lam_type(s, mode) + ", " +
+                            std::to_string(LYAP_JIT_VOLUME_K) + ">");
+            slots.push_back(&e.volume[mode]);
         }
-        names.push_back("&lyapgb::render_persistent<" + lam_type(s, mode) + ">");
-        names.push_back("&lyapgb::volume_sweep<" + lam_type(s, mode) + ", " + std::to_string(LYAP_JIT_VOLUME_K) +
-                        ">");
     }
     const char *src = "#include \"lyap_kernels.cuh\"\n";
     nvrtcProgram prog = nullptr;
@@ -248,11 +256,8 @@ void compile_entry(Entry &e, const Spec &s, int kind)
         e.error = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(ce);
         return;
     }
-    for (int mode = 0; mode < 2; mode++) {
-        const size_t per = prop ? 1 : 2;
-        ce = cudaLibraryGetKernel(&e.render[mode], e.lib, lowered[per * mode].c_str());
-        if (ce == cudaSuccess && !prop)
-            ce = cudaLibraryGetKernel(&e.volume[mode], e.lib, lowered[per * mode + 1].c_str());
+    for (size_t i = 0; i < names.size(); i++) {
+        ce = cudaLibraryGetKernel(slots[i], e.lib, lowered[i].c_str());
         if (ce != cudaSuccess) {
             e.error = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(ce);
             return;
@@ -283,25 +288,34 @@ Entry *get_entry(const int32_t *h_seq, uint32_t L, uint32_t settle, std::string 
         return nullptr;
     }
     const Spec s = make_spec(h_seq, L, settle);
-    const std::string key = lam_type(s, 9) + (kind == KIND_PROPOSAL ? "|proposal" : kind == KIND_BATCH ? "|batch" : "");
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (g_nvrtc_state == 0) g_nvrtc_state = g_nvrtc.load() ? 1 : -1;
-    if (g_nvrtc_state < 0) {
-        *why = "NVRTC unavailable: " + g_nvrtc.why;
-        return nullptr;
+    const std::string key = lam_type(s, 9) + (kind == KIND_PROPOSAL ? "|proposal"
+                                              : kind >= KIND_BATCH ? "|batch" + std::to_string(kind - KIND_BATCH)
+                                                                   : "");
+    Entry *e = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        if (g_nvrtc_state == 0) g_nvrtc_state = g_nvrtc.load() ? 1 : -1;
+        if (g_nvrtc_state < 0) {
+            *why = "NVRTC unavailable: " + g_nvrtc.why;
+            return nullptr;
+        }
+        auto it = g_cache.find(key);
+        if (it == g_cache.end()) it = g_cache.emplace(key, std::unique_ptr<Entry>(new Entry())).first;
+        e = it->second.get();   // entries are never removed: the pointer stays valid
     }
-    auto it = g_cache.find(key);
-    if (it == g_cache.end()) {
-        std::unique_ptr<Entry> e(new Entry());
+    // compiled outside the lock, so that different sequences compile in
+    // parallel; callers of the same entry wait for its one compile
+    std::call_once(e->once, [&] {
         compile_entry(*e, s, kind);
+        std::lock_guard<std::mutex> lock(g_mu);
+        e->done = true;
         g_compiles++;
-        it = g_cache.emplace(key, std::move(e)).first;
-    }
-    if (!it->second->ok) {
-        *why = it->second->error;
+    });
+    if (!e->ok) {
+        *why = e->error;
         return nullptr;
     }
-    return it->second.get();
+    return e;
 }
 
 }  // namespace
@@ -350,7 +364,7 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
 int jit_batch_kernel(const int32_t *h_seq, uint32_t L, uint32_t settle, uint32_t mode, cudaKernel_t *kernel,
                      std::string *why)
 {
-    Entry *e = get_entry(h_seq, L, settle, why, KIND_BATCH);
+    Entry *e = get_entry(h_seq, L, settle, why, KIND_BATCH + (int)(mode & 1u));
     if (!e) return 0;
     *kernel = e->render[mode & 1u];
     return 1;
@@ -399,7 +413,7 @@ extern "C" int lyap_jit_info(char *buf, size_t cap)
                     " env=" + (jit_disabled_by_env() ? "off" : "on") + " compiled=" + std::to_string(g_compiles) +
                     " launches=" + std::to_string(g_launches) + " cached=" + std::to_string(g_cache.size());
     for (auto &kv : g_cache)
-        if (!kv.second->ok) s += "\nerror: " + kv.second->error.substr(0, 400);
+        if (kv.second->done && !kv.second->ok) s += "\nerror: " + kv.second->error.substr(0, 400);
     if (buf && cap) {
         strncpy(buf, s.c_str(), cap - 1);
         buf[cap - 1] = 0;

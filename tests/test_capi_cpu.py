@@ -199,7 +199,7 @@ def test_abi_struct_sizes_match_c(tmp_path):
         "LyapNetTrainOptions": (capi.LyapNetTrainOptions, ["steps", "lr", "seed", "box_lo", "box_hi", "h_loss"]),
         "LyapVolumeExt": (capi.LyapVolumeExt, ["variant", "d_stats", "flags", "h_seq"]),
         "LyapRequest": (capi.LyapRequest, ["prm", "d_seq", "d_counts", "seq_len", "flags"]),
-        "LyapBatchOptions": (capi.LyapBatchOptions, ["autotune", "flags", "d_stats"]),
+        "LyapBatchOptions": (capi.LyapBatchOptions, ["autotune", "flags", "d_stats", "jit_groups"]),
         "LyapBatchInfo": (capi.LyapBatchInfo, ["candidates", "specialised", "tuned_ms"]),
     }
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "lyap_gb300.h"', "int main(void) {"]
@@ -294,3 +294,40 @@ def test_net_entry_argument_errors():
     assert e.value.code == capi.LYAP_ERR_SEQUENCE
     with pytest.raises(capi.LyapError, match="batch"):
         capi.net_train(prm, np.array([0, 1, -1], dtype=np.int32), batch=100)
+
+
+def test_batch_options_checked():
+    """LyapBatchOptions: jit_groups above LYAP_BATCH_JIT_GROUPS_MAX is refused
+    before any device work; a caller built without jit_groups passes the
+    shorter size, which the size check accepts (the call then fails on the
+    request's null buffers instead)."""
+    q = capi.LyapRequest()
+    arr = (capi.LyapRequest * 1)(q)
+    h = ctypes.c_void_p()
+    opt = capi.LyapBatchOptions(jit_groups=capi.BATCH_JIT_GROUPS_MAX + 1)
+    rc = capi.lib.lyap_batch_create(arr, 1, ctypes.byref(opt), ctypes.byref(h))
+    assert rc == capi.LYAP_ERR_INVALID_ARG and "jit_groups" in capi.last_error(), capi.last_error()
+    short = capi.LyapBatchOptions()
+    short.size = capi.LyapBatchOptions.jit_groups.offset
+    rc = capi.lib.lyap_batch_create(arr, 1, ctypes.byref(short), ctypes.byref(h))
+    assert rc == capi.LYAP_ERR_INVALID_ARG and "request 0" in capi.last_error(), capi.last_error()
+    bad = capi.LyapBatchOptions()
+    bad.size = 12
+    rc = capi.lib.lyap_batch_create(arr, 1, ctypes.byref(bad), ctypes.byref(h))
+    assert rc == capi.LYAP_ERR_INVALID_ARG and "LyapBatchOptions.size" in capi.last_error()
+
+
+def test_mirrored_constants_match_the_header():
+    """Every numeric LYAP_* constant of include/lyap_gb300.h that the ctypes
+    mirror defines (under its name without the prefix, or with it) has the
+    header's value."""
+    import re
+    text = open(os.path.join(ROOT, "include", "lyap_gb300.h")).read()
+    checked = 0
+    for name, value in re.findall(r"^#define\s+LYAP_([A-Z0-9_]+)\s+\(?(-?\d+)u?\)?\s*(?:/\*.*)?$", text, re.M):
+        for attr in (name, "LYAP_" + name):
+            if hasattr(capi, attr) and isinstance(getattr(capi, attr), int):
+                assert getattr(capi, attr) == int(value), (attr, getattr(capi, attr), value)
+                checked += 1
+                break
+    assert checked >= 30

@@ -108,7 +108,7 @@ def test_one_sequence_batch_runs_the_specialised_kernel(variant):
     info = db.batch.info()
     if not capi.jit_info()[0]:
         pytest.skip("NVRTC unavailable")
-    assert info.specialised == 1
+    assert info.specialised == len(wls)
     for wl, bf in zip(wls, db.frames):
         f = DeviceFrame(wl, device=dev, counts=True)
         f.run(variant)
@@ -118,5 +118,43 @@ def test_one_sequence_batch_runs_the_specialised_kernel(variant):
         assert torch.equal(bf.d_counts, f.d_counts), wl.name
     off = DeviceBatch(wls, device=dev, variant=variant, autotune=False, counts=True, flags=capi.FLAG_NO_JIT)
     assert off.batch.info().specialised == 0
-    mixed = DeviceBatch(_small_batch(), device=dev, variant=variant, autotune=False)
-    assert mixed.batch.info().specialised == 0
+
+
+def _cost(wl):
+    return wl.width * wl.height * (wl.params.settle + wl.params.accum) * max(1.0, wl.params.depth)
+
+
+@pytest.mark.parametrize("variant", [capi.VARIANT_PLAIN, capi.VARIANT_PRODUCT])
+def test_mixed_batch_compiles_its_heaviest_sequence_groups(variant):
+    """Requests that share a sequence form a group; the batch compiles its
+    kernel for the heaviest groups (jit_groups of them) and runs each as a
+    launch of its own, the rest on the library's kernel.  Every request gets
+    lyap_render's bytes whichever kernel ran it."""
+    dev = torch.device("cuda:0")
+    wls = _one_sequence_batch("ABCCABB")[:4] + _one_sequence_batch("CAB")[:3] + _small_batch()[:3]
+    wls[0].width, wls[0].height = 96, 80   # the first group is the heaviest
+    groups = {}
+    for wl in wls:
+        key = (wl.seq, wl.params.settle % len(wl.seq))
+        groups.setdefault(key, []).append(wl)
+    heavy = max(groups.values(), key=lambda g: sum(_cost(w) for w in g))
+    one = DeviceBatch(wls, device=dev, variant=variant, autotune=False, counts=True, jit_groups=1)
+    one.run()
+    torch.cuda.synchronize()
+    if not capi.jit_info()[0]:
+        pytest.skip("NVRTC unavailable")
+    assert one.batch.info().specialised == len(heavy)
+    every = DeviceBatch(wls, device=dev, variant=variant, autotune=False, counts=True)
+    every.run()
+    torch.cuda.synchronize()
+    total = sum(_cost(w) for w in wls)
+    eligible = [g for g in groups.values() if sum(_cost(w) for w in g) * 200 >= total]
+    assert every.batch.info().specialised == sum(len(g) for g in eligible)
+    for i, wl in enumerate(wls):
+        f = DeviceFrame(wl, device=dev, counts=True)
+        f.run(variant)
+        torch.cuda.synchronize()
+        for bf in (one.frames[i], every.frames[i]):
+            assert torch.equal(bf.d_rgba, f.d_rgba), wl.name
+            assert torch.equal(bf.d_points.view(torch.int32), f.d_points.view(torch.int32)), wl.name
+            assert torch.equal(bf.d_counts, f.d_counts), wl.name
