@@ -418,7 +418,10 @@ int lyap_volume_host(float *out, uint32_t nx, uint32_t ny, uint32_t nz, const fl
  * kernel_calc_render<<<(grid_x, grid_y), (block_x, block_y)>>>
  * (lyap_interactive.cu:711) and kernel_calc_volume<<<grid, block>>>
  * (lyap_calculate.cu:72), with their index and coordinate conventions
- * (image width / volume extents = grid * block).  Plain FP32. */
+ * (image width / volume extents = grid * block).  Plain FP32.
+ * kernel_calc_render takes blocks of at most 256 threads (the reference's
+ * 16 x 16); larger ones are LYAP_ERR_INVALID_ARG here (a <<<>>> launch of
+ * them fails to launch). */
 int lyap_kernel_calc_render(uint32_t grid_x, uint32_t grid_y, uint32_t block_x, uint32_t block_y,
                             RGBA *d_rgba, LyapPoint *d_points, const LyapCam *cam, const LyapParams *prm,
                             int32_t *d_seq, LyapLight *d_lights, uint32_t n_lights, void *stream);

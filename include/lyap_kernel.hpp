@@ -23,6 +23,7 @@
 
 // kernel.cu:500 -- one pixel per thread position; points[x + y*W] and
 // rgba[x + y*W] with W = gridDim.x*blockDim.x; a miss writes an all-NaN point.
+// Blocks of at most 256 threads (the reference's launch is 16 x 16).
 LYAP_KERNEL_EXPORT __global__ void kernel_calc_render(RGBA *rgba, LyapPoint *points, LyapCam cam, LyapParams prm, int *seq,
                                    LyapLight *lights, unsigned int num_lights);
 

@@ -174,8 +174,22 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t mask, uint32_t n)
 // Helper results of one sample round, per warp: the helper of rank k among
 // the lanes without a ray posts its lambda values and skip / fallback bits
 // in slot k; the owner of the ray reads its helpers' slots in order.  Both
-// render kernels run at most 128 threads per block (their launch bounds).
+// persistent kernels run at most 128 threads per block (their launch
+// bounds), 1-D; the reference-shaped kernel_calc_render runs 2-D blocks of
+// up to 256 threads (its round: BLOCK2D).
 constexpr uint32_t ROUND_WARPS = (LYAP_RENDER_THREADS > 128 ? LYAP_RENDER_THREADS : 128) / 32;
+constexpr uint32_t ROUND_WARPS_2D = 256 / 32;
+
+// The thread's lane and warp in its block: 1-D blocks by threadIdx.x, any
+// block (BLOCK2D) by its linear index, of which warps are runs of 32.
+template <bool BLOCK2D>
+__device__ __forceinline__ void lane_warp(uint32_t &lane, uint32_t &warp)
+{
+    const uint32_t tid =
+        BLOCK2D ? threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z) : threadIdx.x;
+    lane = tid & 31u;
+    warp = tid >> 5;
+}
 
 __device__ __forceinline__ void store_point(LyapPoint *dst, const Ray &r, bool hit)
 {
@@ -378,14 +392,15 @@ __device__ __forceinline__ uint32_t sample_kind(const Ray &r)
 // samples.  Helper lane (owner, j) takes the owner's j-th sample ahead; the
 // owner feeds the results to its state machine in order and drops the rest
 // once the ray leaves that phase (or a proposal run is rewound).
-template <bool PROP, class Lam>
+template <bool PROP, class Lam, bool BLOCK2D = false>
 __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uint32_t amask, const Lam &lam,
                                             const LyapParams &prm, const bool spec_ok, const bool bracket_mode,
                                             const PropGrid &pg, LaneStats &st)
 {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    __shared__ float slot_l[ROUND_WARPS][32];
-    __shared__ uint32_t slot_b[ROUND_WARPS][32];
+    uint32_t lane, warp;
+    lane_warp<BLOCK2D>(lane, warp);
+    __shared__ float slot_l[BLOCK2D ? ROUND_WARPS_2D : ROUND_WARPS][32];
+    __shared__ uint32_t slot_b[BLOCK2D ? ROUND_WARPS_2D : ROUND_WARPS][32];
     uint32_t emask = 0, imask = 0, ne = 0, ni = 0, maxj = 0;
     bool helper = false;
     uint32_t owner = lane, offset = 0, rank = 0;

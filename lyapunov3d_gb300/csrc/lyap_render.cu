@@ -118,10 +118,17 @@ using namespace lyapgb;
 // launch shape: pixel (x, y) = (blockIdx*blockDim + threadIdx), index
 // x + y * gridDim.x * blockDim.x, no bounds beyond the grid (as the
 // reference).  The block's warps share the block's pixels through a
-// shared-memory counter, so a warp stays full until its block runs dry.
+// shared-memory counter, so a warp stays full until its block runs dry;
+// then, when the block is whole warps (the reference's 16 x 16 is eight)
+// and the step length is fixed, lanes without a ray take samples ahead for
+// the rays still running in their warp (sample_round, as the persistent
+// render), so a block's longest ray no longer holds it one sample per round.
 // Plain FP32 lambda; the sequence length is found from its -1 terminator.
-LYAP_KERNEL_EXPORT __global__ void kernel_calc_render(RGBA *rgba, LyapPoint *points, LyapCam cam, LyapParams prm, int *seq,
-                                   LyapLight *lights, unsigned int num_lights)
+// Blocks of at most 256 threads (the reference launches 16 x 16), two
+// resident per SM: 128 registers, no spills.
+LYAP_KERNEL_EXPORT __global__ void __launch_bounds__(256, 2)
+    kernel_calc_render(RGBA *rgba, LyapPoint *points, LyapCam cam, LyapParams prm, int *seq, LyapLight *lights,
+                       unsigned int num_lights)
 {
     __shared__ uint32_t next;
     __shared__ uint32_t period;
@@ -137,9 +144,15 @@ LYAP_KERNEL_EXPORT __global__ void kernel_calc_render(RGBA *rgba, LyapPoint *poi
     const uint32_t lane = threadIdx.x & 31u;   // lanes of a block are consecutive in tid
     const uint32_t nitems = blockDim.x * blockDim.y;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const SeqInfo si = seq_setup(seq, period, prm);
+    const RuntimeLambda<MODE_PLAIN> lam(seq, period, prm);
     const CamRays cr = cam_rays(cam);
     LaneStats st = {};
+    // sampling ahead needs whole warps (its ballots and shuffles span 32
+    // lanes) and a slot table for each of the block's warps
+    const uint32_t nthreads = blockDim.x * blockDim.y * blockDim.z;
+    const bool whole_warps = (nthreads % 32u) == 0 && nthreads / 32u <= ROUND_WARPS_2D;
+    const bool spec_ok = whole_warps && prm.jitter == 0.0f && prm.nearMultiplier == 1.0f;
+    const PropGrid no_prop = {};
     Ray r;
     uint32_t ind = 0;
     bool active = false, drained = (threadIdx.z != 0);   // the reference's 2-D launch shape
@@ -172,17 +185,22 @@ LYAP_KERNEL_EXPORT __global__ void kernel_calc_render(RGBA *rgba, LyapPoint *poi
                 }
             }
         }
-        if (__ballot_sync(wmask, active) == 0) break;
-        V3 Q = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
-        bool skipped, fallback;
-        const float lam = eval_lambda<MODE_PLAIN>(Q.x, Q.y, Q.z, si, skipped, fallback);
-        if (active) {
-            const int res = ray_advance(r, lam, prm);
-            if (res != RAY_CONTINUE) {
-                finish_pixel(rgba, points, nullptr, ind, r, res == RAY_HIT, cr.C, lights, num_lights,
-                             LYAP_LIGHT_SPOT, st);
-                active = false;
-            }
+        const uint32_t amask = __ballot_sync(wmask, active);
+        if (amask == 0) break;
+        int res;
+        if (whole_warps) {
+            res = sample_round<false, RuntimeLambda<MODE_PLAIN>, true>(r, active, amask, lam, prm, spec_ok, false,
+                                                                       no_prop, st);
+        } else {
+            V3 Q = active ? ray_sample_point(r) : v3(3.0f, 3.0f, 3.0f);
+            bool skipped, fallback;
+            const float l = lam(Q.x, Q.y, Q.z, skipped, fallback);
+            res = active ? ray_advance(r, l, prm) : RAY_CONTINUE;
+        }
+        if (active && res != RAY_CONTINUE) {
+            finish_pixel(rgba, points, nullptr, ind, r, res == RAY_HIT, cr.C, lights, num_lights, LYAP_LIGHT_SPOT,
+                         st);
+            active = false;
         }
     }
 }
@@ -198,8 +216,9 @@ extern "C" int lyap_kernel_calc_render(uint32_t grid_x, uint32_t grid_y, uint32_
     if (!cam || !prm || !d_seq || !d_rgba || !d_points || (n_lights && !d_lights))
         return set_error(LYAP_ERR_INVALID_ARG, "lyap_kernel_calc_render: null pointer");
     if (n_lights > LYAP_MAX_LIGHTS) return set_error(LYAP_ERR_INVALID_ARG, "lyap_kernel_calc_render: too many lights");
-    if (!grid_x || !grid_y || !block_x || !block_y || (uint64_t)block_x * block_y > 1024)
-        return set_error(LYAP_ERR_INVALID_ARG, "lyap_kernel_calc_render: bad launch shape");
+    if (!grid_x || !grid_y || !block_x || !block_y || (uint64_t)block_x * block_y > 256)
+        return set_error(LYAP_ERR_INVALID_ARG, "lyap_kernel_calc_render: bad launch shape (blocks of at most 256 "
+                                               "threads)");
     kernel_calc_render<<<dim3(grid_x, grid_y), dim3(block_x, block_y), 0, (cudaStream_t)stream>>>(
         d_rgba, d_points, *cam, *prm, d_seq, d_lights, n_lights);
     cudaError_t e = cudaGetLastError();
