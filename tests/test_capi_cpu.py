@@ -180,6 +180,11 @@ def test_drop_in_launcher_argument_errors():
     assert L.lyap_kernel_calc_render(1, 1, 64, 64, ctypes.c_void_p(8), ctypes.c_void_p(8), ctypes.byref(cam),
                                      ctypes.byref(prm), ctypes.c_void_p(8), ctypes.c_void_p(8), 1, None) == \
         capi.LYAP_ERR_INVALID_ARG
+    # blocks of more than 256 threads (the kernel is compiled for two of 256 per SM)
+    assert L.lyap_kernel_calc_render(1, 1, 32, 16, ctypes.c_void_p(8), ctypes.c_void_p(8), ctypes.byref(cam),
+                                     ctypes.byref(prm), ctypes.c_void_p(8), ctypes.c_void_p(8), 1, None) == \
+        capi.LYAP_ERR_INVALID_ARG
+    assert "at most 256" in capi.last_error()
     g = (ctypes.c_uint32 * 3)(1, 1, 0)
     b = (ctypes.c_uint32 * 3)(8, 8, 8)
     assert L.lyap_kernel_calc_volume(g, b, ctypes.c_void_p(8), ctypes.byref(prm), ctypes.c_void_p(8), None) == \

@@ -296,3 +296,19 @@ def test_directional_light_model(dev, oracle):
     i = np.clip(nd, 0, 1)
     expect_r = np.clip(np.floor(255.0 * (L.diffuseColor.x * (i * L.diffusePower) + L.ambient.x)), 0, 255)
     assert np.max(np.abs(rgba[..., 0][hit].astype(int) - expect_r[hit].astype(int))) <= 1
+
+
+@pytest.mark.parametrize("block", [(8, 8), (12, 12), (16, 8), (32, 8)])
+def test_dropin_block_shapes_give_lyap_render_bytes(dev, block):
+    """kernel_calc_render samples ahead only in blocks of whole warps (8x8,
+    16x8, 32x8); a 12x12 block (144 threads) takes the one-sample loop.
+    Either way every pixel gets lyap_render's bytes."""
+    wl = scenes.small_render(96)
+    f = DeviceFrame(wl, device=dev)
+    f.run(capi.VARIANT_PLAIN)
+    d_rgba2, d_pts2 = torch.empty_like(f.d_rgba), torch.empty_like(f.d_points)
+    capi.kernel_calc_render((96 // block[0], 96 // block[1]), block, d_rgba2, d_pts2, f.cam, f.prm, f.d_seq,
+                            f.d_lights, len(f.lights))
+    torch.cuda.synchronize()
+    assert torch.equal(f.d_rgba, d_rgba2)
+    assert torch.equal(f.d_points.view(torch.int32), d_pts2.view(torch.int32))
