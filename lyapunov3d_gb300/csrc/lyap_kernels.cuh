@@ -473,6 +473,88 @@ __device__ __forceinline__ int sample_round(Ray &r, const bool active, const uin
     return res;
 }
 
+// The owner's consumption of a round's samples while its ray marches with a
+// fixed step (no proposal): samples 0 and 1 are its own pair, then two per
+// helper pair k, in slot k * ne + idx.  ray_advance would take them one by
+// one; here the lane keeps only what depends on the order -- the sample
+// count, the a / c sums, the near flag, t and the cap and box-exit checks --
+// and takes each sample's position from where it was evaluated (the helpers
+// stepped P exactly as the march steps it).  The sample at which the march
+// stops (at or below the opaque threshold, or NaN) goes through ray_advance
+// itself, on the ray as it stands there.  Same ray state, same statistics.
+__device__ __forceinline__ int consume_march(Ray &r, float l0, float l1, uint32_t bits, V3 Q1, uint32_t nh,
+                                             uint32_t ne, uint32_t idx, const float2 *slot_l,
+                                             const uint32_t *slot_b, const float4 *slot_p,
+                                             const LyapParams &prm, bool bracket_mode, LaneStats &st)
+{
+    const float opaque = prm.opaqueThreshold, chaos = prm.chaosThreshold, near_t = prm.nearThreshold;
+    float a = r.a, c = r.c, t = r.t, tprev = r.tprev, lam_prev = r.l;
+    uint32_t nm = r.nm, phase = r.phase;
+    bool near = r.near;
+    V3 Pa = r.P, Pb = Q1;   // positions of the current pair's two samples
+    float la = l0, lb = l1;
+    uint32_t bb = bits;
+    auto store = [&](V3 P) {
+        r.a = a;
+        r.c = c;
+        r.t = t;
+        r.tprev = tprev;
+        r.l = lam_prev;
+        r.nm = nm;
+        r.phase = phase;
+        r.near = near;
+        r.dt = near ? r.Ndt : r.Fdt;
+        r.P = P;
+    };
+    for (uint32_t j = 0;; j++) {
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float lam = h ? lb : la;
+            const V3 P = h ? Pb : Pa;
+            st.samples += 1;
+            st.skipped += (bb >> h) & 1u;
+            st.fallback += (bb >> (2 + h)) & 1u;
+            st.spec_used += j ? 1u : 0u;
+            if (!(lam > opaque)) {
+                // the march stops here: the whole step on the ray as it stands
+                store(P);
+                return ray_advance<false>(r, lam, prm, bracket_mode, nullptr);
+            }
+            nm += 1;
+            lam_prev = lam;
+            if (phase == PH_MARCH) {
+                if (lam > chaos) c = c + lam;
+                else a = a + lam;
+                near = lam <= near_t;
+            }
+            if (nm >= r.cap) {
+                store(P);
+                return RAY_MISS;
+            }
+            const float step = near ? r.Ndt : r.Fdt;
+            tprev = t;
+            t = t + step;
+            if (t > r.t1) {
+                store(P + r.V * step);
+                return RAY_MISS;
+            }
+            phase = PH_MARCH;
+            if (h == 1 && j >= nh) {
+                store(P + r.V * step);
+                return RAY_CONTINUE;
+            }
+        }
+        const uint32_t slot = j * ne + idx;
+        const float2 v = slot_l[slot];
+        la = v.x;
+        lb = v.y;
+        bb = slot_b[slot];
+        const float4 pa = slot_p[2 * slot], pb = slot_p[2 * slot + 1];
+        Pa = v3(pa.x, pa.y, pa.z);
+        Pb = v3(pb.x, pb.y, pb.z);
+    }
+}
+
 // Paired rounds (RenderTuning::pairs): every lane evaluates two lambda samples
 // per round as one packed evaluation (Lam::eval<2>; the product form runs both
 // on FP32 pairs, fma.rn.f32x2).  Slot 0 is what sample_round evaluates; slot 1
@@ -490,6 +572,7 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     __shared__ float2 slot_l[ROUND_WARPS][32];
     __shared__ uint32_t slot_b[ROUND_WARPS][32];
+    __shared__ float4 slot_p[PROP ? 1 : ROUND_WARPS][PROP ? 1 : 64];   // the helpers' sample positions
     // can this ray's next positions be known before its current sample's lambda?
     const bool ahead = active && known_ahead(r, fixed_step);
     // the ray's own second slot also takes its next hone step, assuming the
@@ -543,6 +626,10 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
         if (helper) {
             slot_l[warp][rank] = make_float2(lv[0], lv[1]);
             slot_b[warp][rank] = bits;
+            if constexpr (!PROP) {
+                slot_p[warp][2 * rank] = make_float4(Q0.x, Q0.y, Q0.z, 0.0f);
+                slot_p[warp][2 * rank + 1] = make_float4(Q1.x, Q1.y, Q1.z, 0.0f);
+            }
         }
         __syncwarp();
     }
@@ -556,6 +643,12 @@ __device__ __forceinline__ int sample_round_pair(Ray &r, const bool active, cons
         if (ne && ahead) {
             idx = __popc(emask & ((1u << lane) - 1u));
             nh = idx < ni ? (ni - idx + ne - 1) / ne : 0u;
+        }
+        if constexpr (!PROP) {
+            // a fixed-step march: the lean consumption (ahead_self holds)
+            if (kind == 1u && fixed_step)
+                return consume_march(r, lv[0], lv[1], bits, Q1, nh, ne, idx, slot_l[warp], slot_b[warp],
+                                     slot_p[warp], prm, bracket_mode, st);
         }
         float l0 = lv[0], l1 = lv[1];
         // the own pair (its second sample only when taken ahead), then the
