@@ -250,7 +250,11 @@ cudaError_t plan_parts(LyapBatch &b, const LyapRequest *reqs, uint32_t max_group
         }
     };
     std::vector<std::thread> pool;
-    for (size_t t = 1; t < nthreads; t++) pool.emplace_back(work);
+    try {
+        for (size_t t = 1; t < nthreads; t++) pool.emplace_back(work);
+    } catch (...) {
+        // no more threads: the calling thread compiles what is left
+    }
     if (nthreads) work();
     for (auto &t : pool) t.join();
     std::vector<char> special(b.n_jobs, 0);
