@@ -469,10 +469,10 @@ typedef struct {
 /* Requests with the same sequence (and settle count mod its period) form a
  * group; the batch kernel is compiled at run time (NVRTC, parallel host
  * threads, cached for the process) for the heaviest groups that carry at
- * least 1/200 of the batch's estimated cost, and each such group runs as a
+ * least 1/1000 of the batch's estimated cost, and each such group runs as a
  * launch of its own in the batch's graph; the other requests run the
  * library's kernel.  A batch of one sequence is one specialised launch. */
-#define LYAP_BATCH_JIT_GROUPS_DEFAULT 64u
+#define LYAP_BATCH_JIT_GROUPS_DEFAULT 255u
 #define LYAP_BATCH_JIT_GROUPS_MAX 255u
 
 typedef struct {

@@ -46,7 +46,7 @@ MAX_LIGHTS = 16
  STAT_NET_TIMEOUTS, STAT_T_START, STAT_T_DRAIN, STAT_T_END, STAT_PROPOSAL_REWOUND, STAT_TAIL_HANDOVERS) = range(21)
 STAT_COUNT = 21
 PROPOSAL_GRID_DEFAULT = 64
-BATCH_JIT_GROUPS_DEFAULT = 64
+BATCH_JIT_GROUPS_DEFAULT = 255
 BATCH_JIT_GROUPS_MAX = 255
 # the proposal margin the library's users are pointed to: the smallest of the
 # measured margins at which the 1080p bench frame keeps >= 99.9 % of its

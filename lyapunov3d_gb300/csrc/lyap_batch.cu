@@ -16,7 +16,7 @@
 // Sequences.  Requests that share a sequence (and settle count mod its
 // period) form a group.  For the heaviest groups -- up to
 // LyapBatchOptions.jit_groups (default LYAP_BATCH_JIT_GROUPS_DEFAULT), each
-// carrying at least 1/200 of the batch's estimated cost -- the batch kernel
+// carrying at least 1/1000 of the batch's estimated cost -- the batch kernel
 // is compiled for the group's sequence at run time (ConstLambda, paired
 // rounds), the compiles running in parallel host threads; the other
 // requests run the library's kernel for any sequence (RuntimeLambda).  Each
@@ -230,7 +230,7 @@ cudaError_t plan_parts(LyapBatch &b, const LyapRequest *reqs, uint32_t max_group
         double c = 0;
         for (uint32_t j : g.second) c += b.cost[j];
         const uint32_t L = (uint32_t)g.first.first.size() - 1;
-        if (L <= LYAP_JIT_MAX_PERIOD && (groups.size() == 1 || c * 200.0 >= total))
+        if (L <= LYAP_JIT_MAX_PERIOD && (groups.size() == 1 || c * 1000.0 >= total))
             cand.push_back(Group{&g.first, &g.second, c, reqs[g.second[0]].prm.settle, nullptr});
     }
     std::stable_sort(cand.begin(), cand.end(), [](const Group &a, const Group &c) { return a.cost > c.cost; });
