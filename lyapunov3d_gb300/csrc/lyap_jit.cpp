@@ -119,7 +119,8 @@ bool jit_disabled_by_env()
 }
 
 // Resident render blocks per SM the specialised kernel is compiled for
-// (its register cap); LYAP_JIT_RENDER_BLOCKS=4..8 overrides the default.
+// (its register cap, blocks of LYAP_RENDER_THREADS_JIT threads);
+// LYAP_JIT_RENDER_BLOCKS=2..16 overrides the default.
 // the lambda forms (the kernels' MODE_PLAIN / MODE_PRODUCT; e->render[mode])
 constexpr uint32_t kModePlain = 0, kModeProduct = 1;
 
@@ -221,9 +222,10 @@ void compile_entry(Entry &e, const Spec &s, int kind)
     const std::string vmin = "-DLYAP_VOLUME_MIN_BLOCKS=" + std::to_string(LYAP_JIT_VOLUME_MIN_BLOCKS);
     const std::string pairs0 = "-DLYAP_RENDER_PAIRS_PLAIN=" + std::to_string(jit_render_pairs(kModePlain));
     const std::string pairs1 = "-DLYAP_RENDER_PAIRS_PRODUCT=" + std::to_string(jit_render_pairs(kModeProduct));
+    const std::string rthreads = "-DLYAP_RENDER_THREADS=" + std::to_string(LYAP_RENDER_THREADS_JIT);
     const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-fmad=false", "-lineinfo",
                           "--ptxas-options=-v", rmin0.c_str(), rmin1.c_str(), vmin.c_str(), pairs0.c_str(),
-                          pairs1.c_str()};
+                          pairs1.c_str(), rthreads.c_str()};
     r = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
     size_t ls = 0;
     N.log_size(prog, &ls);

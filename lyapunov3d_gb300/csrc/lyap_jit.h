@@ -8,21 +8,24 @@
 #include "lyap_jobs.h"
 
 // Launch shape of the specialised kernels: with the sequence compiled in,
-// the render kernel fits in 80 registers without spilling (6 blocks of 128
-// threads per SM, against 4 for the precompiled kernel) and the volume sweep
-// evaluates LYAP_JIT_VOLUME_K voxels per thread in 64 registers (4 blocks of
-// 256 threads per SM).
+// the plain render fits in 80 registers without spilling (3 blocks of 256
+// threads per SM, against 4 of 128 for the precompiled kernel) and the volume
+// sweep evaluates LYAP_JIT_VOLUME_K voxels per thread in 64 registers (4
+// blocks of 256 threads per SM).  The renders run blocks of 256 threads: the
+// end-of-frame hand-over works within a block, and 8 warps give it more to
+// balance than 4 at the same warps per SM (about 1 % faster 1080p frames,
+// the time after the drain 3.5 against 3.7-4.7 ms).
 #define LYAP_JIT_MAX_PERIOD 32
-#define LYAP_JIT_RENDER_MIN_BLOCKS 6
+#define LYAP_JIT_RENDER_MIN_BLOCKS 3
 // paired rounds (two samples per lane, packed FP32 pairs) in the specialised
 // product-form render: 5-10 % faster 1080p frames than one sample per lane
-// at 6 blocks/SM; with 4 blocks/SM (up to 128 registers) 1-4 % faster than
-// with 5 or 6.  The plain form is MUFU-bound: packing gains it nothing and
+// at 24 warps/SM; with 16 warps/SM (up to 128 registers) 1-4 % faster than
+// with 20 or 24.  The plain form is MUFU-bound: packing gains it nothing and
 // the lower occupancy costs it, so it keeps one sample per lane.
 #define LYAP_JIT_RENDER_PAIRS_PRODUCT 1
 #define LYAP_JIT_RENDER_PAIRS_PLAIN 0
-#define LYAP_JIT_RENDER_MIN_BLOCKS_PAIRS 4
-#define LYAP_RENDER_THREADS_JIT 128
+#define LYAP_JIT_RENDER_MIN_BLOCKS_PAIRS 2
+#define LYAP_RENDER_THREADS_JIT 256
 #define LYAP_JIT_VOLUME_K 2
 #define LYAP_JIT_VOLUME_MIN_BLOCKS 4
 #define LYAP_VOLUME_THREADS_JIT 256
