@@ -77,7 +77,7 @@ struct LyapBatch {
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;   // [0]: the fork; [1 + i]: part i done
     // chosen launch shape
-    uint32_t tile_w = 16, tile_h = 16, tiles_per_chunk = 1, blocks_per_sm = 3, threads = 128;
+    uint32_t tile_w = 16, tile_h = 16, tiles_per_chunk = 1, blocks_per_sm = 3, threads = LYAP_BATCH_THREADS;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     LyapBatchInfo info;

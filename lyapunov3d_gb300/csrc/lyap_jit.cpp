@@ -118,9 +118,9 @@ bool jit_disabled_by_env()
     return v && (strcmp(v, "0") == 0 || strcmp(v, "off") == 0);
 }
 
-// Resident render blocks per SM the specialised kernel is compiled for
-// (its register cap, blocks of LYAP_RENDER_THREADS_JIT threads);
-// LYAP_JIT_RENDER_BLOCKS=2..16 overrides the default.
+// Resident render blocks per SM the specialised kernel is compiled for (its
+// register cap, blocks of jit_render_threads threads);
+// LYAP_JIT_RENDER_BLOCKS=1..16 overrides the default.
 // the lambda forms (the kernels' MODE_PLAIN / MODE_PRODUCT; e->render[mode])
 constexpr uint32_t kModePlain = 0, kModeProduct = 1;
 
@@ -138,9 +138,15 @@ int jit_render_min_blocks(uint32_t mode)
     const char *v = getenv("LYAP_JIT_RENDER_BLOCKS");
     if (v) {
         const int n = atoi(v);
-        if (n >= 2 && n <= 16) return n;
+        if (n >= 1 && n <= 16) return n;
     }
     return jit_render_pairs(mode) ? LYAP_JIT_RENDER_MIN_BLOCKS_PAIRS : LYAP_JIT_RENDER_MIN_BLOCKS;
+}
+
+// threads per block of the specialised render of lambda form `mode`
+int jit_render_threads(uint32_t mode)
+{
+    return jit_render_pairs(mode) ? LYAP_JIT_RENDER_THREADS_PAIRS : LYAP_JIT_RENDER_THREADS;
 }
 
 std::string hex64(uint64_t v)
@@ -222,10 +228,11 @@ void compile_entry(Entry &e, const Spec &s, int kind)
     const std::string vmin = "-DLYAP_VOLUME_MIN_BLOCKS=" + std::to_string(LYAP_JIT_VOLUME_MIN_BLOCKS);
     const std::string pairs0 = "-DLYAP_RENDER_PAIRS_PLAIN=" + std::to_string(jit_render_pairs(kModePlain));
     const std::string pairs1 = "-DLYAP_RENDER_PAIRS_PRODUCT=" + std::to_string(jit_render_pairs(kModeProduct));
-    const std::string rthreads = "-DLYAP_RENDER_THREADS=" + std::to_string(LYAP_RENDER_THREADS_JIT);
+    const std::string rthr0 = "-DLYAP_RENDER_THREADS_PLAIN=" + std::to_string(jit_render_threads(kModePlain));
+    const std::string rthr1 = "-DLYAP_RENDER_THREADS_PRODUCT=" + std::to_string(jit_render_threads(kModeProduct));
     const char *opts[] = {"--gpu-architecture=sm_103a", "-std=c++17", "-fmad=false", "-lineinfo",
                           "--ptxas-options=-v", rmin0.c_str(), rmin1.c_str(), vmin.c_str(), pairs0.c_str(),
-                          pairs1.c_str(), rthreads.c_str()};
+                          pairs1.c_str(), rthr0.c_str(), rthr1.c_str()};
     r = N.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
     size_t ls = 0;
     N.log_size(prog, &ls);
@@ -335,7 +342,7 @@ int jit_launch_render(const RenderJob &job, uint32_t mode, const int32_t *h_seq,
         *why = "no device";
         return 0;
     }
-    if (threads == 0) threads = LYAP_RENDER_THREADS_JIT;
+    if (threads == 0) threads = (uint32_t)jit_render_threads(mode);
     if (blocks_per_sm == 0) {
         int dev = 0, nb = 0;
         cudaGetDevice(&dev);

@@ -11,12 +11,14 @@
 // the plain render fits in 80 registers without spilling (3 blocks of 256
 // threads per SM, against 4 of 128 for the precompiled kernel) and the volume
 // sweep evaluates LYAP_JIT_VOLUME_K voxels per thread in 64 registers (4
-// blocks of 256 threads per SM).  The renders run blocks of 256 threads: the
-// end-of-frame hand-over works within a block, and 8 warps give it more to
-// balance than 4 at the same warps per SM (about 1 % faster 1080p frames,
-// the time after the drain 3.5 against 3.7-4.7 ms).
+// blocks of 256 threads per SM).  The end-of-frame hand-over of the render
+// works within a block, so the paired product render runs one block of 512
+// threads per SM (16 warps, up to 128 registers): 12.69-12.72 ms per 1080p
+// frame against 13.00-13.07 with 2 blocks of 256 and about 13.15 with 4 of
+// 128, the same warps per SM each time.
 #define LYAP_JIT_MAX_PERIOD 32
 #define LYAP_JIT_RENDER_MIN_BLOCKS 3
+#define LYAP_JIT_RENDER_THREADS 256
 // paired rounds (two samples per lane, packed FP32 pairs) in the specialised
 // product-form render: 5-10 % faster 1080p frames than one sample per lane
 // at 24 warps/SM; with 16 warps/SM (up to 128 registers) 1-4 % faster than
@@ -24,8 +26,8 @@
 // the lower occupancy costs it, so it keeps one sample per lane.
 #define LYAP_JIT_RENDER_PAIRS_PRODUCT 1
 #define LYAP_JIT_RENDER_PAIRS_PLAIN 0
-#define LYAP_JIT_RENDER_MIN_BLOCKS_PAIRS 2
-#define LYAP_RENDER_THREADS_JIT 256
+#define LYAP_JIT_RENDER_MIN_BLOCKS_PAIRS 1
+#define LYAP_JIT_RENDER_THREADS_PAIRS 512
 #define LYAP_JIT_VOLUME_K 2
 #define LYAP_JIT_VOLUME_MIN_BLOCKS 4
 #define LYAP_VOLUME_THREADS_JIT 256

@@ -25,6 +25,18 @@
 #ifndef LYAP_RENDER_THREADS
 #define LYAP_RENDER_THREADS 128
 #endif
+// per lambda form: threads per block of the persistent render (its
+// end-of-frame hand-over works within a block)
+#ifndef LYAP_RENDER_THREADS_PRODUCT
+#define LYAP_RENDER_THREADS_PRODUCT LYAP_RENDER_THREADS
+#endif
+#ifndef LYAP_RENDER_THREADS_PLAIN
+#define LYAP_RENDER_THREADS_PLAIN LYAP_RENDER_THREADS
+#endif
+// the batch kernel's blocks (its warps switch requests, they hand nothing over)
+#ifndef LYAP_BATCH_THREADS
+#define LYAP_BATCH_THREADS 128
+#endif
 #ifndef LYAP_RENDER_MIN_BLOCKS
 #define LYAP_RENDER_MIN_BLOCKS 4
 #endif
@@ -177,7 +189,9 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t mask, uint32_t n)
 // persistent kernels run at most 128 threads per block (their launch
 // bounds), 1-D; the reference-shaped kernel_calc_render runs 2-D blocks of
 // up to 256 threads (its round: BLOCK2D).
-constexpr uint32_t ROUND_WARPS = (LYAP_RENDER_THREADS > 128 ? LYAP_RENDER_THREADS : 128) / 32;
+constexpr uint32_t ROUND_THREADS_MAX =
+    LYAP_RENDER_THREADS_PRODUCT > LYAP_RENDER_THREADS_PLAIN ? LYAP_RENDER_THREADS_PRODUCT : LYAP_RENDER_THREADS_PLAIN;
+constexpr uint32_t ROUND_WARPS = (ROUND_THREADS_MAX > LYAP_BATCH_THREADS ? ROUND_THREADS_MAX : LYAP_BATCH_THREADS) / 32;
 constexpr uint32_t ROUND_WARPS_2D = 256 / 32;
 
 // The thread's lane and warp in its block: 1-D blocks by threadIdx.x, any
@@ -802,13 +816,17 @@ struct RenderTuning {
     static constexpr bool product = Lam::mode == MODE_PRODUCT;
     static constexpr bool pairs = product ? LYAP_RENDER_PAIRS_PRODUCT != 0 : LYAP_RENDER_PAIRS_PLAIN != 0;
     static constexpr int min_blocks = product ? LYAP_RENDER_MIN_BLOCKS_PRODUCT : LYAP_RENDER_MIN_BLOCKS_PLAIN;
+    static constexpr int threads = product ? LYAP_RENDER_THREADS_PRODUCT : LYAP_RENDER_THREADS_PLAIN;
+    // the batch kernel, in blocks of LYAP_BATCH_THREADS: the same registers per thread
+    static constexpr int batch_min_blocks =
+        (min_blocks * threads + LYAP_BATCH_THREADS - 1) / LYAP_BATCH_THREADS;
 };
 
 // PROP: the learned proposal's grid (job.prop) decides which march
 // positions are skipped; the host launches this instantiation only with a
 // grid and a fixed step length (jitter 0, near multiplier 1).
 template <class Lam, bool PROP = false>
-__global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_blocks)
+__global__ void __launch_bounds__(RenderTuning<Lam>::threads, RenderTuning<Lam>::min_blocks)
     render_persistent(const __grid_constant__ RenderJob job, uint32_t *__restrict__ work_counter,
                       unsigned long long *__restrict__ stats)
 {
@@ -953,7 +971,7 @@ struct BatchTables {
 // request of the batch has the same sequence, ConstLambda compiled for it at
 // run time, which runs paired rounds as the single-frame render does.
 template <class Lam>
-__global__ void __launch_bounds__(LYAP_RENDER_THREADS, RenderTuning<Lam>::min_blocks)
+__global__ void __launch_bounds__(LYAP_BATCH_THREADS, RenderTuning<Lam>::batch_min_blocks)
     render_batch(const __grid_constant__ BatchTables tb, uint32_t *__restrict__ chunk_counter,
                  unsigned long long *__restrict__ stats)
 {
