@@ -185,10 +185,11 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t mask, uint32_t n)
 
 // Helper results of one sample round, per warp: the helper of rank k among
 // the lanes without a ray posts its lambda values and skip / fallback bits
-// in slot k; the owner of the ray reads its helpers' slots in order.  Both
-// persistent kernels run at most 128 threads per block (their launch
-// bounds), 1-D; the reference-shaped kernel_calc_render runs 2-D blocks of
-// up to 256 threads (its round: BLOCK2D).
+// in slot k; the owner of the ray reads its helpers' slots in order.  The
+// persistent render runs 1-D blocks of LYAP_RENDER_THREADS_PRODUCT /
+// _PLAIN threads, the batch kernel of LYAP_BATCH_THREADS (their launch
+// bounds); the reference-shaped kernel_calc_render runs 2-D blocks of up to
+// 256 threads (its round: BLOCK2D).
 constexpr uint32_t ROUND_THREADS_MAX =
     LYAP_RENDER_THREADS_PRODUCT > LYAP_RENDER_THREADS_PLAIN ? LYAP_RENDER_THREADS_PRODUCT : LYAP_RENDER_THREADS_PLAIN;
 constexpr uint32_t ROUND_WARPS = (ROUND_THREADS_MAX > LYAP_BATCH_THREADS ? ROUND_THREADS_MAX : LYAP_BATCH_THREADS) / 32;
@@ -967,9 +968,10 @@ struct BatchTables {
 // lambda loop must be uniform), so it continues with the next chunk while
 // that belongs to the same request and otherwise lets its rays run out --
 // idle lanes speculate for the rays still running -- before switching.  Lam
-// is RuntimeLambda (any sequences; the library's kernel) or, when every
-// request of the batch has the same sequence, ConstLambda compiled for it at
-// run time, which runs paired rounds as the single-frame render does.
+// is RuntimeLambda (any sequences; the library's kernel) or, for the
+// requests of one sequence group of the batch, ConstLambda compiled for that
+// sequence at run time, which runs paired rounds as the single-frame render
+// does.
 template <class Lam>
 __global__ void __launch_bounds__(LYAP_BATCH_THREADS, RenderTuning<Lam>::batch_min_blocks)
     render_batch(const __grid_constant__ BatchTables tb, uint32_t *__restrict__ chunk_counter,
